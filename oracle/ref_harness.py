@@ -1,0 +1,110 @@
+"""Drive the compat-built reference CPU engine (test infrastructure only).
+
+Imports the modules that ``oracle/build_ref.py`` compiled into
+``oracle/_ref/FiniteDifference`` and builds a Heston engine the way the
+reference's ``HestonFiniteDifferenceEngine`` does. ``heston.py`` itself cannot
+be imported under Python 3 (print statements, numexpr, pylab), so its
+coefficient dict (heston.py:302-333), boundary dict (heston.py:335-359) and
+grid construction (heston.py:380-406) are restated here in Python 3 and handed
+to the reference ``FiniteDifferenceEngineADI`` unchanged.
+
+Only usable in a container where the reference tree was built; nothing in the
+product or in the GPU tests imports this module.
+"""
+import contextlib
+import io
+import itertools
+import os
+import sys
+
+import numpy as np
+
+_REF = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_ref")
+
+
+def available():
+    return os.path.isdir(os.path.join(_REF, "FiniteDifference"))
+
+
+def _import():
+    if _REF not in sys.path:
+        sys.path.insert(0, _REF)
+    # FiniteDifferenceEngine.pyx:411 calls itertools.izip (Python 2).
+    if not hasattr(itertools, "izip"):
+        itertools.izip = zip
+    import FiniteDifference.FiniteDifferenceEngine as FD  # noqa: E402
+    import FiniteDifference.BandedOperator as BO  # noqa: E402
+    import FiniteDifference.utils as U  # noqa: E402
+    from FiniteDifference.Grid import Grid  # noqa: E402
+    return FD, BO, U, Grid
+
+
+def heston_mesh(S0, K, v0, nS, nv, spot_max, var_max, spotdensity=7.0, varexp=4.0):
+    """heston.py:384-406: v = exponential_space(0, v0, var_max, varexp, nv),
+    S = sinh_space(K, spot_max, spotdensity, nS); spot pinned to S0."""
+    FD, BO, U, Grid = _import()
+    with contextlib.redirect_stdout(io.StringIO()):
+        vars_ = U.exponential_space(0.0, v0, var_max, varexp, nv, force_exact=True)
+        spots = U.sinh_space(K, spot_max, spotdensity, nS, force_exact=True)
+    spots = np.array(spots, dtype=float)
+    spots[np.argmin(np.abs(spots - S0))] = S0
+    return spots, np.array(vars_, dtype=float)
+
+
+def heston_engine(S0, K, r, v0, kappa, theta, sigma, rho, spots, vars_):
+    """A reference FiniteDifferenceEngineADI with the Heston PDE (heston.py:302-359)."""
+    FD, BO, U, Grid = _import()
+
+    def mu_s(t, *dim):
+        return r * dim[0]
+
+    def gamma2_s(t, *dim):
+        return 0.5 * dim[1] * dim[0] ** 2
+
+    def mu_v(t, *dim):
+        if np.isscalar(dim[0]):
+            if dim[0] == 0:
+                return 0
+        ret = kappa * (theta - dim[1])
+        ret[dim[0] == 0] = 0
+        return ret
+
+    def gamma2_v(t, *dim):
+        if np.isscalar(dim[0]):
+            if dim[0] == 0:
+                return 0
+        ret = 0.5 * sigma ** 2 * dim[1]
+        ret[dim[0] == 0] = 0
+        return ret
+
+    def cross(t, *dim):
+        return rho * sigma * dim[0] * dim[1]
+
+    coefficients = {(): lambda t: -r, (0,): mu_s, (0, 0): gamma2_s,
+                    (1,): mu_v, (1, 1): gamma2_v, (0, 1): cross}
+    boundaries = {
+        (0,): ((0, lambda t, *dim: 0.0), (1, lambda t, *dim: 1.0)),
+        (0, 0): ((0, lambda t, *dim: 0.0), (None, lambda t, *dim: 1.0)),
+        (1,): ((None, lambda t, *dim: None), (None, lambda t, *dim: None)),
+        (1, 1): ((1, lambda t, *dim: 0), (None, lambda t, *dim: None)),
+    }
+    schemes = {(0,): [{"scheme": "center"}], (1,): [{"scheme": "center"}]}
+    grid = Grid([spots, vars_], initializer=lambda *x: np.maximum(x[0] - K, 0))
+    F = FD.FiniteDifferenceEngineADI(grid, coefficients=coefficients,
+                                     boundaries=boundaries, schemes=schemes)
+    with contextlib.redirect_stdout(io.StringIO()):
+        F.init()
+    return F
+
+
+def price_index(spots, vars_, S0, v0):
+    """heston.py:461-465: bisect on meshes rounded to 4 decimals."""
+    from bisect import bisect_left
+    ids = bisect_left(list(np.round(spots, decimals=4)), np.round(S0, decimals=4))
+    idv = bisect_left(list(np.round(vars_, decimals=4)), np.round(v0, decimals=4))
+    return ids, idv
+
+
+def quiet(fn, *a, **k):
+    with contextlib.redirect_stdout(io.StringIO()):
+        return fn(*a, **k)
