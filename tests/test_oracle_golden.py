@@ -1,0 +1,90 @@
+"""The C oracle against the reference's own outputs (tests/golden/*.npz).
+
+The fixtures were produced by the reference CPU engine (see
+tests/golden/make_golden.py). The oracle restates that engine, so its
+operators must match bit for bit and its grids to rounding.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from oracle import analytic
+
+HV_THETA = 0.5 + np.sqrt(3) / 6
+
+
+def test_operators_bitwise(golden):
+    g = golden("operators")
+    r, kappa, theta, sigma, rho = g["params"]
+    ops = O.heston_operators(g["S"], g["v"], r, kappa, theta, sigma, rho)
+    np.testing.assert_array_equal(ops["A0"], g["A0"])
+    np.testing.assert_array_equal(ops["A1"], g["A1"])
+    np.testing.assert_array_equal(ops["R0"], g["R0"])
+    np.testing.assert_array_equal(ops["R1"], g["R1"])
+    np.testing.assert_array_equal(ops["status"], g["status"])
+    n0, n1 = g["S"].size, g["v"].size
+    M = np.zeros((n0 * n1, n0 * n1))
+    for i in range(n0):
+        for j in range(n1):
+            for a in (-1, 0, 1):
+                for b in (-1, 0, 1):
+                    ii, jj = i + a, j + b
+                    if 0 <= ii < n0 and 0 <= jj < n1:
+                        M[i * n1 + j, ii * n1 + jj] += ops["M9"][i * n1 + j, (a + 1) * 3 + (b + 1)]
+    np.testing.assert_array_equal(M, g["M"])
+
+
+SCHED = {
+    "douglas": lambda n, dt: [("douglas", n, dt, 0.5)],
+    "hv": lambda n, dt: [("hv", n, dt, HV_THETA)],
+    "implicit": lambda n, dt: [("implicit", n, dt, 1.0)],
+    "smooth": lambda n, dt: [("implicit", 2, dt * 0.5, 1.0), ("hv", n - 1, dt, 0.6)],
+}
+
+
+@pytest.mark.parametrize("case", range(12))
+def test_solves_match_reference(golden, case):
+    g = golden("solves")
+    key = str(g["cases"][case])
+    r, kappa, theta, sigma, rho = g["case_params"][case]
+    scheme = key.split("_", 1)[1]
+    out = O.heston_solve(g["S"], g["v"], r, kappa, theta, sigma, rho, g["V0"],
+                         SCHED[scheme](20, 0.01))
+    ref = g[key]
+    scale = np.abs(ref).max()
+    assert np.abs(out - ref).max() <= 1e-12 * scale, key
+
+
+def test_config1_full_grid(golden):
+    g = golden("config1")
+    S, v = g["S"], g["v"]
+    V0 = np.maximum(S[:, None] - 100.0, 0) * np.ones((1, v.size))
+    n, dt = 150, 1.0 / 150
+    out = O.heston_solve(S, v, 0.06, 1.0, 0.04, 0.2, 0.0, V0,
+                         [("implicit", 2, dt * 0.5, 1.0), ("douglas", n - 1, dt, 0.5)])
+    idx = tuple(g["idx"])
+    # spec tolerances: price 1e-10 relative, grid 1e-9 max-norm
+    assert abs(out[idx] - g["price"]) <= 1e-10 * abs(g["price"])
+    assert np.abs(out - g["V"]).max() <= 1e-9
+
+
+def test_config1_vs_semianalytic(golden):
+    g = golden("config1")
+    cos = analytic.heston_cos(100., 100., 0.06, 0.04, 1.0, 1.0, 0.04, 0.2, 0.0)[0, 0]
+    # the reference's own accuracy bar (tests/test_HestonOptionGPU.py: rtol 1e-3)
+    assert abs(float(g["price"]) - cos) <= 1e-3 * cos
+
+
+def test_blackscholes(golden):
+    g = golden("blackscholes")
+    r, var, K = g["params"]
+    n, dt = 200, 1.0 / 200
+    for name, sched in (("implicit", [("implicit", n, dt, 1.0)]),
+                        ("douglas", [("douglas", n, dt, 0.5)]),
+                        ("hv", [("hv", n, dt, 0.5)]),
+                        ("smooth", [("implicit", 2, dt / 2, 1.0), ("hv", n - 1, dt, 0.6)])):
+        out = O.bs_solve(g["S"], r, var, g["V0"], sched)
+        assert np.abs(out - g[name]).max() <= 1e-11 * np.abs(g[name]).max(), name
+    i = int(np.argmin(np.abs(g["S"] - 100.0)))
+    exact = analytic.bs_call(100.0, K, r, var, 1.0)[0]
+    assert abs(g["douglas"][i] - exact) <= 1e-3 * exact
