@@ -1,0 +1,419 @@
+#!/usr/bin/env python
+"""Benchmark: Heston options/sec of the batched FP64 ADI pricer on one GB300.
+
+Workload (the batched configuration): 4096 Heston calls drawn from a seed,
+uniform in K/S0 in [0.7, 1.3], T in [0.1, 2], r in [0, 0.08], kappa in [0.5, 5],
+theta in [0.01, 0.16], sigma in [0.1, 1], rho in [-0.9, 0], v0 in [0.01, 0.16];
+uneven grids nS in {64, 96, ..., 512}, nv in {32, 48, ..., 256}; nt = 200
+(two implicit half-steps, then 199 Hundsdorfer-Verwer steps at
+theta = 1/2 + sqrt(3)/6). One step = pricing the whole batch once: build every
+option's operators on the device, reset the state to the payoff and run the
+200 time steps (one CUDA graph), then read the prices. Inputs are synthetic
+(there is no public dataset); state arrays (~1.4 GB) exceed L2.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line (rank 0).
+"""
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Heston options/sec at <=1e-3 abs err: batched ADI vs plain ADI vs surrogate"
+UNIT = "options/s"
+HV_THETA = 0.5 + np.sqrt(3.0) / 6.0
+
+# Algorithmic state traffic (bytes per grid point) and FP64 work (flops per
+# grid point, an FMA counts 2) of one launch of each stage kernel.
+STAGE_BYTES = {"explicit_hv0": 32, "explicit_hv3": 40, "spot_solve": 24, "var_solve_y2": 16,
+               "var_solve_v": 16, "explicit_implicit": 16, "var_solve_implicit": 16,
+               "spot_solve_implicit": 16}
+STAGE_FLOPS = {"explicit_hv0": 40, "explicit_hv3": 60, "spot_solve": 7, "var_solve_y2": 6,
+               "var_solve_v": 6, "explicit_implicit": 16, "var_solve_implicit": 7,
+               "spot_solve_implicit": 7}
+
+
+def workload(n_options, seed, nt=200):
+    """Seeded config: per option (params, nS, nv)."""
+    rng = np.random.default_rng(seed)
+    S0 = 100.0
+    K = S0 * rng.uniform(0.7, 1.3, n_options)
+    T = rng.uniform(0.1, 2.0, n_options)
+    r = rng.uniform(0.0, 0.08, n_options)
+    kappa = rng.uniform(0.5, 5.0, n_options)
+    theta = rng.uniform(0.01, 0.16, n_options)
+    sigma = rng.uniform(0.1, 1.0, n_options)
+    rho = rng.uniform(-0.9, 0.0, n_options)
+    v0 = rng.uniform(0.01, 0.16, n_options)
+    nS = rng.choice(np.arange(64, 513, 32), n_options)
+    nv = rng.choice(np.arange(32, 257, 16), n_options)
+    # group equal grid sizes so neighbouring lines of the arena have equal length
+    order = np.lexsort((nv, nS))
+    cols = [K, T, r, kappa, theta, sigma, rho, v0, nS, nv]
+    K, T, r, kappa, theta, sigma, rho, v0, nS, nv = [c[order] for c in cols]
+    return dict(S0=S0, K=K, T=T, r=r, kappa=kappa, theta=theta, sigma=sigma, rho=rho, v0=v0,
+                nS=nS.astype(np.int32), nv=nv.astype(np.int32), nt=nt)
+
+
+def _mesh_one(args):
+    from fd_adi_gb300 import mesh
+    S0, K, v0, nS, nv = args
+    return mesh.heston_meshes(S0, K, v0, int(nS), int(nv), 8.0 * K, 5.0)
+
+
+def meshes_for(w, idx=None):
+    idx = range(len(w["K"])) if idx is None else idx
+    jobs = [(w["S0"], w["K"][k], w["v0"][k], w["nS"][k], w["nv"][k]) for k in idx]
+    if len(jobs) > 64:
+        import multiprocessing as mp
+        with mp.get_context("spawn").Pool(min(16, os.cpu_count() or 1)) as pool:
+            return pool.map(_mesh_one, jobs, chunksize=32)
+    return [_mesh_one(j) for j in jobs]
+
+
+def params_of(w, idx=None):
+    idx = range(len(w["K"])) if idx is None else idx
+    return [(w["r"][k], w["kappa"][k], w["theta"][k], w["sigma"][k], w["rho"][k]) for k in idx]
+
+
+def payoffs(w, meshes, idx=None):
+    idx = list(range(len(w["K"])) if idx is None else idx)
+    return [np.maximum(m[0][:, None] - w["K"][k], 0.0) * np.ones((1, m[1].size))
+            for k, m in zip(idx, meshes)]
+
+
+class Clocks(object):
+    """nvidia-smi samples during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(mx)) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+def fp64_peak(torch):
+    """FP64 FMA throughput of this device, measured with the library's probe."""
+    from fd_adi_gb300 import _lib
+    dev = torch.cuda.current_device()
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    blocks, threads, iters = sms * 8, 256, 4096
+    out = torch.empty(blocks * threads, dtype=torch.float64, device="cuda")
+    flops = ctypes.c_double()
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    best = 0.0
+    for _ in range(4):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        _lib.call("fdadi_fp64_probe", ctypes.c_void_p(out.data_ptr()), blocks, threads, iters,
+                  ctypes.byref(flops), st)
+        e1.record()
+        e1.synchronize()
+        best = max(best, flops.value / (e0.elapsed_time(e1) * 1e-3))
+    return best / 1e12
+
+
+def stage_times(batch, V, torch):
+    """Average device time per launch of every stage kernel over one full
+    run, launched stage by stage with CUDA events on the batch's stream."""
+    from fd_adi_gb300 import _lib
+    s = batch.struct
+    seq = []
+    for _ in range(s.implicit_steps):
+        seq += ["explicit_implicit", "var_solve_implicit", "spot_solve_implicit"]
+    for _ in range(s.n_steps):
+        seq += ["explicit_hv0", "spot_solve", "var_solve_y2", "explicit_hv3", "spot_solve",
+                "var_solve_v"]
+    stream = batch.stream
+    acc, cnt = {}, {}
+    evs = []
+    with torch.cuda.stream(stream):
+        for name in seq:
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            _lib.call("fdadi_heston_stage", ctypes.byref(s),
+                      ctypes.c_void_p(batch.workspace.data_ptr()), batch.workspace_bytes,
+                      ctypes.c_void_p(V.data_ptr()), _lib.STAGE[name],
+                      ctypes.c_void_p(stream.cuda_stream))
+            e1.record(stream)
+            evs.append((name, e0, e1))
+    stream.synchronize()
+    for name, e0, e1 in evs:
+        acc[name] = acc.get(name, 0.0) + e0.elapsed_time(e1)
+        cnt[name] = cnt.get(name, 0) + 1
+    return {k: (acc[k] / cnt[k], cnt[k], acc[k]) for k in acc}
+
+
+def cpu_baseline(w, n_sample, kind_pref="port"):
+    """Oracle (C restatement, OpenMP over options) or the compat-built
+    reference on this host's cores, on the first n_sample options."""
+    from oracle import oracle as O
+    n = len(w["K"])
+    idx = sorted(set(np.linspace(0, n - 1, n_sample).astype(int).tolist()))
+    meshes = meshes_for(w, idx)
+    V0 = payoffs(w, meshes, idx)
+    nt = w["nt"]
+    scheds = [[("implicit", 2, w["T"][k] / nt / 2, 1.0), ("hv", nt - 1, w["T"][k] / nt, HV_THETA)]
+              for k in idx]
+    cores = os.cpu_count() or 1
+    O.build()
+    t0 = time.perf_counter()
+    O.heston_batch(meshes, params_of(w, idx), V0, scheds, nthreads=cores)
+    dt = time.perf_counter() - t0
+    pts = float(sum(int(w["nS"][k]) * int(w["nv"][k]) for k in idx)) * nt
+    # the sample's grid-point-step rate, converted to options of the full
+    # workload's mean grid size
+    mean_pts = float(np.mean(w["nS"].astype(np.int64) * w["nv"])) * nt
+    return {"value": pts / dt / mean_pts, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "%d options evenly spaced through the seeded %d-option workload "
+                      "(%.3g grid-point-steps), all %d cores, %.1f s: %.3g grid-point-steps/s, "
+                      "scaled by the workload's mean grid size" % (len(idx), n, pts, cores, dt,
+                                                                    pts / dt)}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    w = workload(args.options, args.seed)
+    rates = []
+    for s in range(args.warmup + args.steps):
+        cb = cpu_baseline(w, args.ref_sample)
+        if s >= args.warmup:
+            rates.append(cb["value"])
+    value = float(np.mean(rates))
+    cb["value"] = value
+    times = [args.options / r for r in rates]
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": float(np.mean(times)) * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": config_block(args, w),
+            "cpu_baseline": cb,
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def config_block(args, w):
+    return {"workload": "batched Heston calls, uneven grids, HV nt=200 with Rannacher start",
+            "options_per_gpu": int(len(w["K"])), "nt": int(w["nt"]),
+            "grid_points": int(np.sum(w["nS"].astype(np.int64) * w["nv"])),
+            "nS": "uniform {64..512 step 32}", "nv": "uniform {32..256 step 16}",
+            "scheme": "2 implicit half-steps + 199 HV steps, theta=1/2+sqrt(3)/6",
+            "seed": args.seed, "l2": "state arrays larger than L2 (no flush needed)",
+            "parallelism": "dp%d (options sharded, no collective)" % args.gpus}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--options", type=int, default=4096)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--ref-sample", type=int, default=32)
+    ap.add_argument("--cpu-sample", type=int, default=32)
+    ap.add_argument("--no-extras", action="store_true")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import torch
+    import torch.distributed as dist
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from fd_adi_gb300 import _lib
+    from fd_adi_gb300.batch import HestonBatch
+    _lib.load()
+
+    # weak scaling: every rank prices its own seeded batch of args.options
+    w = workload(args.options, args.seed + rank)
+    meshes = meshes_for(w)
+    params = params_of(w)
+    nt = w["nt"]
+    dts = (w["T"] / nt).tolist()
+    batch = HestonBatch(params, meshes, scheme="hv", n_steps=nt - 1, dt=dts, theta=HV_THETA,
+                        implicit_steps=2, implicit_dt_factor=0.5, graph=True)
+    # device-resident inputs (value) and pinned host copies (e2e)
+    V0_dev = batch.pack(payoffs(w, meshes))
+    V = torch.empty_like(V0_dev)
+    h_spots = batch.spots.cpu().pin_memory()
+    h_vars = batch.vars.cpu().pin_memory()
+    h_params = batch.params.cpu().pin_memory()
+    h_dt = batch.dt.cpu().pin_memory()
+    h_V0 = V0_dev.cpu().pin_memory()
+    flat_idx = batch.flat_index()
+    prices = torch.empty(batch.n, dtype=torch.float64, device="cuda")
+    h_prices = torch.empty(batch.n, dtype=torch.float64).pin_memory()
+    stream = batch.stream
+
+    def step_device():
+        with torch.cuda.stream(stream):
+            batch._prepare()
+            V.copy_(V0_dev, non_blocking=True)
+            batch.run(V)
+            batch.gather(V, flat_idx, prices)
+
+    def step_e2e():
+        with torch.cuda.stream(stream):
+            batch.spots.copy_(h_spots, non_blocking=True)
+            batch.vars.copy_(h_vars, non_blocking=True)
+            batch.params.copy_(h_params, non_blocking=True)
+            batch.dt.copy_(h_dt, non_blocking=True)
+            V.copy_(h_V0, non_blocking=True)
+            batch._prepare()
+            batch.run(V)
+            batch.gather(V, flat_idx, prices)
+            h_prices.copy_(prices, non_blocking=True)
+
+    def timed(fn, k):
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(k):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        ms = e0.elapsed_time(e1) / k
+        if world > 1:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms
+
+    for _ in range(args.warmup):
+        step_device()
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    clocks.start()
+    time.sleep(0.3)
+    ms = timed(step_device, args.steps)
+    clk = clocks.stop()
+    step_e2e()
+    torch.cuda.synchronize()
+    ms_e2e = timed(step_e2e, max(1, args.steps))
+
+    n_total = args.options * world
+    value = n_total / (ms * 1e-3)
+    e2e_value = n_total / (ms_e2e * 1e-3)
+    h2d = sum(t.numel() * t.element_size() for t in (h_spots, h_vars, h_params, h_dt, h_V0))
+    d2h = h_prices.numel() * 8
+    launches = args.steps * (batch.launches_per_run + 3 + 1)
+
+    out = None
+    if rank == 0:
+        P = batch.total_points
+        st = stage_times(batch, V, torch)
+        dom = max(st, key=lambda k: st[k][2])
+        avg_ms = st[dom][0]
+        hbm_peak, peak_src = measured_peaks()
+        ach = STAGE_BYTES[dom] * P / (avg_ms * 1e-3) / 1e9
+        fp64 = fp64_peak(torch)
+        fp_ach = STAGE_FLOPS[dom] * P / (avg_ms * 1e-3) / 1e12
+        pts_steps = float(P) * nt
+        out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+               "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+               "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+               "dtype": "f64", "data": "synthetic", "config": config_block(args, w),
+               "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                       "d2h_bytes_per_step": int(d2h), "ms_per_step": ms_e2e},
+               "gpu_launches": int(launches),
+               "grid_point_steps_per_s": pts_steps * world / (ms * 1e-3),
+               "roofline": {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": hbm_peak,
+                            "unit": "GB/s", "frac": ach / hbm_peak, "traffic": None,
+                            "peak_source": peak_src,
+                            "bytes_per_point": STAGE_BYTES[dom],
+                            "avg_launch_ms": avg_ms, "launches": st[dom][1]},
+               "fp64_pipe": {"kernel": dom, "achieved": fp_ach, "peak": fp64,
+                             "unit": "TFLOP/s", "frac": fp_ach / fp64,
+                             "peak_source": "measured live (fdadi_fp64_probe)",
+                             "flops_per_point": STAGE_FLOPS[dom]},
+               "stage_ms": {k: round(v[0], 4) for k, v in st.items()},
+               "clocks": clk}
+        if not args.no_extras:
+            out["cpu_baseline"] = cpu_baseline(w, args.cpu_sample)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(out))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

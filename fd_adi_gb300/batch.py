@@ -1,0 +1,171 @@
+"""Batched Heston pricing on the fused engine (fdadi_heston_* in include/fdadi.h).
+
+Thousands of options with different parameters and uneven grids are packed
+into one arena and advanced together: every time step is a handful of
+launches over the whole batch, optionally replayed from a CUDA graph. The
+reference prices one option per engine with dozens of launches per step
+(FiniteDifferenceEngineGPU.pyx:502-562); this has no reference counterpart
+beyond the per-option results, which match the reference CPU engine.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from . import mesh as _mesh
+
+SCHEMES = {"douglas": _lib.SCHEME_DOUGLAS, "hv": _lib.SCHEME_HV,
+           "hundsdorferverwer": _lib.SCHEME_HV}
+HV_THETA = 0.5 + np.sqrt(3.0) / 6.0
+
+
+def option_params(opt):
+    """(r, kappa, theta, sigma, rho) of a HestonOption or a 5-sequence."""
+    if hasattr(opt, "params"):
+        return opt.params()
+    return tuple(float(x) for x in opt)
+
+
+class HestonBatch(object):
+    """A prepared batch: operators and line-solve factors of every option
+    built on the device once; ``run`` advances a packed state arena.
+
+    options: HestonOption objects or (r, kappa, theta, sigma, rho) tuples.
+    meshes:  list of (spots, vars) numpy arrays, one per option.
+    dt:      per-option main step (scalar or sequence).
+    Schedule: ``implicit_steps`` fully implicit steps of dt*implicit_dt_factor,
+    then ``n_steps`` of ``scheme`` ("douglas" or "hv") at ``theta``."""
+
+    def __init__(self, options, meshes, scheme="hv", n_steps=1, dt=0.01, theta=HV_THETA,
+                 implicit_steps=0, implicit_dt_factor=0.5, barrier=None, drop_zero_mixed=True,
+                 graph=False, device=None, stream=None):
+        self.device = device or torch.device("cuda", torch.cuda.current_device())
+        n = len(options)
+        if n == 0 or len(meshes) != n:
+            raise ValueError("need one mesh per option")
+        self.options = options
+        self.n = n
+        self.n0 = np.array([np.asarray(m[0]).size for m in meshes], dtype=np.int32)
+        self.n1 = np.array([np.asarray(m[1]).size for m in meshes], dtype=np.int32)
+        self.sizes = self.n0.astype(np.int64) * self.n1
+        self.p_off = np.concatenate([[0], np.cumsum(self.sizes)]).astype(np.int64)
+        self.total_points = int(self.p_off[-1])
+        dev = self.device
+        self.spots = torch.as_tensor(np.concatenate([np.asarray(m[0], np.float64) for m in meshes]),
+                                     device=dev)
+        self.vars = torch.as_tensor(np.concatenate([np.asarray(m[1], np.float64) for m in meshes]),
+                                    device=dev)
+        self.params = torch.as_tensor(np.array([option_params(o) for o in options],
+                                               dtype=np.float64).reshape(n, 5), device=dev)
+        self.dt = torch.as_tensor(np.broadcast_to(np.asarray(dt, dtype=np.float64), (n,)).copy(),
+                                  device=dev)
+        bar = np.zeros(n, dtype=np.int32) if barrier is None else np.asarray(barrier, np.int32)
+        self.barrier = torch.as_tensor(bar, device=dev)
+        self.graph = bool(graph)
+        if stream is None:
+            stream = torch.cuda.Stream(device=dev) if self.graph else torch.cuda.current_stream(dev)
+        self.stream = stream
+        flags = (_lib.HESTON_DROP_ZERO_MIXED if drop_zero_mixed else 0) | \
+                (_lib.HESTON_GRAPH if self.graph else 0)
+        self._n0_host = self.n0.copy()
+        self._n1_host = self.n1.copy()
+        self.struct = _lib.HestonBatch(
+            n, SCHEMES[scheme], int(n_steps), int(implicit_steps), float(theta),
+            float(implicit_dt_factor), flags, 0,
+            self._n0_host.ctypes.data, self._n1_host.ctypes.data,
+            self.spots.data_ptr(), self.vars.data_ptr(), self.params.data_ptr(),
+            self.dt.data_ptr(), self.barrier.data_ptr())
+        lib = _lib.load()
+        nbytes = lib.fdadi_heston_workspace_bytes(ctypes.byref(self.struct))
+        if nbytes < 0:
+            raise ValueError("bad batch: " + _lib.last_error())
+        self.workspace_bytes = int(nbytes)
+        self.workspace = torch.empty(self.workspace_bytes, dtype=torch.uint8, device=dev)
+        self._prepare()
+
+    @classmethod
+    def from_options(cls, options, nspots, nvols, spot_max_factor=8.0, var_max=5.0,
+                     spotdensity=7.0, varexp=4.0, **kw):
+        """Meshes as the reference Heston engine builds them
+        (heston.py:384-406) with S_max = spot_max_factor * K."""
+        ns = np.broadcast_to(np.asarray(nspots), (len(options),))
+        nv = np.broadcast_to(np.asarray(nvols), (len(options),))
+        meshes = [_mesh.heston_meshes(o.spot, o.strike, o.variance.value, int(a), int(b),
+                                      spot_max_factor * o.strike, var_max, spotdensity, varexp)
+                  for o, a, b in zip(options, ns, nv)]
+        return cls(options, meshes, **kw), meshes
+
+    def _sptr(self):
+        return ctypes.c_void_p(self.stream.cuda_stream)
+
+    def _prepare(self):
+        with torch.cuda.stream(self.stream):
+            _lib.call("fdadi_heston_prepare", ctypes.byref(self.struct),
+                      ctypes.c_void_p(self.workspace.data_ptr()), self.workspace_bytes,
+                      self._sptr())
+
+    @property
+    def launches_per_run(self):
+        return int(_lib.load().fdadi_heston_launch_count(ctypes.byref(self.struct)))
+
+    def pack(self, grids):
+        """Host grids (one [n0, n1] array per option) -> device arena."""
+        flat = np.concatenate([np.asarray(g, dtype=np.float64).reshape(-1) for g in grids])
+        if flat.size != self.total_points:
+            raise ValueError("Dimension mismatch: %d grid points for a %d-point batch"
+                             % (flat.size, self.total_points))
+        return torch.as_tensor(flat, device=self.device)
+
+    def unpack(self, V):
+        h = V.detach().cpu().numpy()
+        return [h[self.p_off[k]:self.p_off[k + 1]].reshape(self.n0[k], self.n1[k])
+                for k in range(self.n)]
+
+    def run(self, V):
+        """Advance the packed state arena V (device, float64) in place."""
+        if V.dtype != torch.float64 or not V.is_cuda or V.numel() != self.total_points:
+            raise ValueError("state must be a CUDA float64 tensor of %d points" % self.total_points)
+        if self.graph:
+            self.stream.wait_stream(torch.cuda.current_stream(self.device))
+        _lib.call("fdadi_heston_run", ctypes.byref(self.struct),
+                  ctypes.c_void_p(self.workspace.data_ptr()), self.workspace_bytes,
+                  ctypes.c_void_p(V.data_ptr()), self._sptr())
+        if self.graph:
+            torch.cuda.current_stream(self.device).wait_stream(self.stream)
+        return V
+
+    def solve(self, grids):
+        """Host grids in, host grids out."""
+        V = self.pack(grids)
+        self.run(V)
+        return self.unpack(V)
+
+    def flat_index(self, meshes=None, points=None):
+        """Arena index of each option's (spot, variance) grid point, by the
+        reference's rounded bisection (FiniteDifferenceEngineGPU.pyx:727-734)."""
+        idx = np.zeros(self.n, dtype=np.int64)
+        spots = self.spots.cpu().numpy()
+        vars_ = self.vars.cpu().numpy()
+        s0 = np.concatenate([[0], np.cumsum(self.n0)])
+        v0 = np.concatenate([[0], np.cumsum(self.n1)])
+        for k, o in enumerate(self.options):
+            S = spots[s0[k]:s0[k + 1]]
+            v = vars_[v0[k]:v0[k + 1]]
+            i, j = _mesh.price_index(S, v, o.spot, o.variance.value)
+            idx[k] = self.p_off[k] + i * self.n1[k] + j
+        return torch.as_tensor(idx, device=self.device)
+
+    def gather(self, V, flat_idx, out=None):
+        if out is None:
+            out = torch.empty(flat_idx.numel(), dtype=torch.float64, device=self.device)
+        _lib.call("fdadi_gather", ctypes.c_void_p(V.data_ptr()),
+                  ctypes.c_void_p(flat_idx.data_ptr()), ctypes.c_void_p(out.data_ptr()),
+                  flat_idx.numel(), ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream))
+        return out
+
+
+def payoff_grids(options, meshes):
+    """Call payoff max(S - K, 0) on each option's grid (heston.py:402)."""
+    return [np.maximum(np.asarray(m[0])[:, None] - o.strike, 0.0) * np.ones((1, np.asarray(m[1]).size))
+            for o, m in zip(options, meshes)]

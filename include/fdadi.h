@@ -1,0 +1,221 @@
+/*
+ * fdadi.h -- C ABI of libfdadi.so, the GB300 (sm_103a) FP64 ADI pricer.
+ *
+ * Every entry point takes plain device pointers, sizes and a CUDA stream
+ * (passed as void*; NULL = legacy default stream) and returns 0 on success or
+ * a nonzero FDADI_E* code; fdadi_last_error() gives the message of the last
+ * failure on the calling thread. Nothing here allocates device memory:
+ * scratch is passed in by the caller (workspace pointers sized by the
+ * *_workspace_bytes queries). All arithmetic is IEEE binary64.
+ *
+ * Grid layout: a 2-D state V[n0][n1] is row-major (n1 contiguous), the
+ * reference domain layout V[iS, iv] (FiniteDifference/Grid.py:35-40). A 1-D
+ * state uses n1 = 1.
+ *
+ * Operator layout: an operator along `axis` acts on `blocks` independent
+ * lines of `block_len = operator_rows / blocks` points. Its diagonals are
+ * row-aligned (sup[r] = A[r, r+1], mid[r] = A[r, r], sub[r] = A[r, r-1]) and
+ * indexed in the reference's flattened block-major order r = b * block_len + k
+ * (the order after the operator axis is rolled last,
+ * FiniteDifference/BandedOperator.pyx:335-337; the GPU reference keeps the same
+ * "cublas" layout, FiniteDifference/BandedOperatorGPU.pyx:651-676). For axis 0
+ * line b is grid column j = b and element k is row i; for axis 1 line b is
+ * grid row i = b and element k is column j.
+ */
+#ifndef FDADI_H
+#define FDADI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FDADI_OK 0
+#define FDADI_E_ARG 1        /* bad argument: sizes, pointers, shapes ("Dimension mismatch") */
+#define FDADI_E_CUDA 2       /* a CUDA runtime call failed */
+#define FDADI_E_WORKSPACE 3  /* workspace too small */
+#define FDADI_E_STATE 4      /* operation not valid in the operator's fold state */
+
+/* fold status codes: the reference's "CANNOT_FOLD", "CAN_FOLD", "FOLDED"
+ * strings (FiniteDifference/BandedOperator.pyx:15-17) */
+#define FDADI_CANNOT_FOLD 0
+#define FDADI_CAN_FOLD 1
+#define FDADI_FOLDED 2
+
+#define FDADI_SCHEME_IMPLICIT 0
+#define FDADI_SCHEME_DOUGLAS 1
+#define FDADI_SCHEME_HV 2
+
+/* library version (major*10000 + minor*100 + patch) */
+int fdadi_version(void);
+
+/* Copies the message of the last failed call on this thread into buf
+ * (NUL-terminated, truncated to len); returns its length. Replaces the
+ * reference's DIE()/std::domain_error text (FiniteDifference/common.h:17-27). */
+int fdadi_last_error(char *buf, size_t len);
+
+/* ------------------------------------------------------------------------ */
+/* Tridiagonal operator: replaces the C++ class _TriBandedOperator          */
+/* (FiniteDifference/_TriBandedOperatorGPU.cuh:21-85) behind                */
+/* BandedOperatorGPU.BandedOperator (FiniteDifference/BandedOperatorGPU.pxd).*/
+/* ------------------------------------------------------------------------ */
+typedef struct fdadi_tri {
+    int64_t operator_rows;        /* N = blocks * block_len */
+    int64_t blocks;
+    int32_t axis;                 /* 0 or 1 */
+    int32_t has_residual;         /* enable_residual() state */
+    int32_t has_low_dirichlet;
+    int32_t has_high_dirichlet;
+    int32_t top_fold_status;      /* FDADI_CANNOT_FOLD / CAN_FOLD / FOLDED */
+    int32_t bottom_fold_status;
+    double *sup, *mid, *sub;      /* [N] row-aligned diagonals */
+    double *R;                    /* [N] residual */
+    double *low_dirichlet;        /* [blocks] values forced on row 0 of each line */
+    double *high_dirichlet;       /* [blocks] values forced on the last row */
+    double *top_factors;          /* [blocks] CAN_FOLD: A[0,2]; FOLDED: fold factor */
+    double *bottom_factors;       /* [blocks] CAN_FOLD: A[L-1,L-3]; FOLDED: fold factor */
+} fdadi_tri_t;
+
+/* y = A x (+ R if has_residual), x with its Dirichlet entries forced first;
+ * a folded operator is unfolded after the product. y may alias x.
+ * Replaces _TriBandedOperator::apply (_TriBandedOperatorGPU.cu:463-553). */
+int fdadi_tri_apply(const fdadi_tri_t *op, const double *x, double *y,
+                    int64_t n0, int64_t n1, void *stream);
+
+/* x <- A^-1 (x_forced - R): Dirichlet entries forced, residual subtracted if
+ * enabled, right-hand side folded, then one Thomas solve per line. A CAN_FOLD
+ * operator is folded on the fly (same linear system). scratch: [N] doubles.
+ * Replaces _TriBandedOperator::solve (_TriBandedOperatorGPU.cu:719-770). */
+int fdadi_tri_solve(const fdadi_tri_t *op, double *x, int64_t n0, int64_t n1,
+                    double *scratch, void *stream);
+
+/* Row r of every diagonal, R and the fold extras scaled by vec[r]; Dirichlet
+ * rows are left alone. Replaces vectorized_scale
+ * (_TriBandedOperatorGPU.cu:1012-1105). If vec is NULL, `scalar` is used for
+ * every row (mul_scalar_from_host, BandedOperatorGPU.pyx:488-501). */
+int fdadi_tri_scale(fdadi_tri_t *op, const double *vec, double scalar, void *stream);
+
+/* mid[r] += value on all rows but Dirichlet rows (residual untouched).
+ * Replaces add_scalar_from_host / add_scalar (_TriBandedOperatorGPU.cu:674-711). */
+int fdadi_tri_add_scalar(fdadi_tri_t *op, double value, void *stream);
+
+/* self += other (same axis, rows, blocks; neither folded): off-diagonals and
+ * R everywhere, main diagonal skipping self's Dirichlet rows, CAN_FOLD
+ * extras added. Replaces add_operator (_TriBandedOperatorGPU.cu:577-671). */
+int fdadi_tri_add_operator(fdadi_tri_t *self, const fdadi_tri_t *other, void *stream);
+
+/* Fold (unfold = 0) or unfold (unfold = 1) the top and/or bottom rows of
+ * every line: one Gaussian-elimination step that removes A[0,2] / A[L-1,L-3].
+ * Updates the status fields of *op. Replaces diagonalize/undiagonalize and
+ * fold_top/fold_bottom (_TriBandedOperatorGPU.cu:836-1009). */
+int fdadi_tri_fold(fdadi_tri_t *op, int32_t top, int32_t bottom, int32_t unfold, void *stream);
+
+/* ------------------------------------------------------------------------ */
+/* Mixed d2/dx0dx1 operator: replaces _CSRBandedOperator                    */
+/* (FiniteDifference/_CSRBandedOperatorGPU.cuh:15-82) and its cuSPARSE csrmv.*/
+/* The reference's 9-point CSR stencil (_CSRBandedOperatorGPU.cu:505-774) is */
+/* the product of two centred first-derivative stencils times a per-point   */
+/* coefficient; it is stored here in that factored form.                   */
+/* ------------------------------------------------------------------------ */
+typedef struct fdadi_mixed {
+    int64_t n0, n1;
+    int32_t has_residual;
+    int32_t reserved;
+    double *coeff;   /* [n0*n1] per-point coefficient (grid order) */
+    double *w0;      /* [3][n0]: A_0[i,i-1], A_0[i,i], A_0[i,i+1] (rows 0, n0-1 zero) */
+    double *w1;      /* [3][n1]: same along axis 1 */
+    double *R;       /* [n0*n1] */
+} fdadi_mixed_t;
+
+/* y = coeff .* (D0 (x) D1) x (+ R). y must not alias x. */
+int fdadi_mixed_apply(const fdadi_mixed_t *op, const double *x, double *y, void *stream);
+
+/* coeff[p] *= vec[p] (or *= scalar if vec is NULL); R scaled too. */
+int fdadi_mixed_scale(fdadi_mixed_t *op, const double *vec, double scalar, void *stream);
+
+/* y = a*y + b*x over n doubles: the SizedArray pluseq/minuseq/minuseq_over2/
+ * timeseq used by the reference GPU loops (FiniteDifference/VecArray.cu:32-116). */
+int fdadi_axpby(double *y, const double *x, double a, double b, int64_t n, void *stream);
+
+/* ------------------------------------------------------------------------ */
+/* Fused batched Heston engine: replaces the per-step call chains of        */
+/* FiniteDifferenceEngineGPU.solve_{implicit,douglas,hundsdorferverwer,     */
+/* smooth}_ (FiniteDifference/FiniteDifferenceEngineGPU.pyx:379-593) with    */
+/* operators built on the device as HestonFiniteDifferenceEngine builds     */
+/* them (FiniteDifferenceEngineGPU.pyx:596-724, heston.py:302-359).         */
+/* ------------------------------------------------------------------------ */
+typedef struct fdadi_heston_batch {
+    int32_t n_options;
+    int32_t scheme;          /* FDADI_SCHEME_DOUGLAS or FDADI_SCHEME_HV (main segment) */
+    int32_t n_steps;         /* main-segment steps */
+    int32_t implicit_steps;  /* fully implicit steps run before the main segment */
+    double theta;            /* main-segment theta */
+    double implicit_dt_factor; /* implicit step = dt * factor (0.5: Rannacher half-steps) */
+    int32_t flags;           /* FDADI_HESTON_* bits */
+    int32_t reserved;
+    const int32_t *n0;       /* HOST [n_options] spot points */
+    const int32_t *n1;       /* HOST [n_options] variance points */
+    const double *spots;     /* DEVICE [sum n0] spot meshes, packed */
+    const double *vars;      /* DEVICE [sum n1] variance meshes, packed */
+    const double *params;    /* DEVICE [n_options][5]: r, kappa, theta, sigma, rho */
+    const double *dt;        /* DEVICE [n_options] main-segment step */
+    const int32_t *barrier;  /* DEVICE [n_options] nonzero: up-and-out (Dirichlet 0 at S_max), or NULL */
+} fdadi_heston_batch_t;
+
+/* drop the mixed operator of options with rho == 0, as the GPU reference
+ * does (FiniteDifferenceEngineGPU.pyx:118-126, 720-724) */
+#define FDADI_HESTON_DROP_ZERO_MIXED 1
+/* capture the time loop in a CUDA graph and launch that */
+#define FDADI_HESTON_GRAPH 2
+
+/* Bytes of device workspace fdadi_heston_prepare/run need for this batch
+ * (operator plans, line tables and stage buffers). */
+int64_t fdadi_heston_workspace_bytes(const fdadi_heston_batch_t *batch);
+
+/* Build every option's operators and line-solve factors into the workspace.
+ * Meshes/params must be on the device. */
+int fdadi_heston_prepare(const fdadi_heston_batch_t *batch, void *workspace,
+                         int64_t workspace_bytes, void *stream);
+
+/* Run the schedule (implicit_steps fully implicit steps of dt*implicit_dt_factor,
+ * then n_steps of the scheme; solve_smooth's Rannacher start is
+ * implicit_steps = 2*s with factor 0.5, FiniteDifferenceEngine.pyx:1010-1016) on
+ * the packed state V (DEVICE [sum n0*n1], option k at offset sum_{m<k} n0*n1),
+ * in place. Requires a prepared workspace. */
+int fdadi_heston_run(const fdadi_heston_batch_t *batch, void *workspace,
+                     int64_t workspace_bytes, double *V, void *stream);
+
+/* out[k] = V[flat_index[k]] for k < n (DEVICE arrays): price read-out. */
+int fdadi_gather(const double *V, const int64_t *flat_index, double *out, int64_t n,
+                 void *stream);
+
+/* Number of kernel launches fdadi_heston_run issues for this batch. */
+int64_t fdadi_heston_launch_count(const fdadi_heston_batch_t *batch);
+
+/* Launch one stage kernel of the time loop (for per-kernel timing; a run is
+ * the sequence these make up). stage: FDADI_STAGE_*. */
+#define FDADI_STAGE_EXPLICIT_DOUGLAS 0
+#define FDADI_STAGE_EXPLICIT_HV0 1
+#define FDADI_STAGE_EXPLICIT_HV3 2
+#define FDADI_STAGE_EXPLICIT_IMPLICIT 3
+#define FDADI_STAGE_SPOT_SOLVE 4        /* W -> W - T (main plan) */
+#define FDADI_STAGE_VAR_SOLVE_TO_Y2 5   /* W -> Y2 (main plan) */
+#define FDADI_STAGE_VAR_SOLVE_TO_V 6    /* W -> V (main plan) */
+#define FDADI_STAGE_VAR_SOLVE_IMPLICIT 7 /* W -> W (implicit plan) */
+#define FDADI_STAGE_SPOT_SOLVE_IMPLICIT 8 /* W -> V (implicit plan) */
+int fdadi_heston_stage(const fdadi_heston_batch_t *batch, void *workspace,
+                       int64_t workspace_bytes, double *V, int32_t stage, void *stream);
+
+/* FP64 throughput probe: a dependent-chain-free DFMA loop on every SM;
+ * writes one value per thread to out (>= blocks*threads doubles) and returns
+ * the number of floating-point operations it issues (2 per DFMA) in *flops.
+ * Used by the benchmark to measure the FP64 roofline on the device. */
+int fdadi_fp64_probe(double *out, int32_t blocks, int32_t threads, int32_t iters,
+                     double *flops, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FDADI_H */

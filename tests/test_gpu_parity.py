@@ -1,0 +1,266 @@
+"""CUDA path against the oracle and the reference's golden outputs.
+
+Tolerances: the spec bar is price within 1e-10 relative and the full
+grid within 1e-9 max-norm of the reference CPU engine; on the small fixtures
+the fused kernels agree to ~1e-13 relative, so those tests use 1e-11 of the
+grid's max to catch semantic slips early.
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+pytestmark = pytest.mark.gpu
+
+from oracle import oracle as O  # noqa: E402
+
+HV_THETA = 0.5 + np.sqrt(3) / 6
+SCHED = {
+    "douglas": lambda n, dt: [("douglas", n, dt, 0.5)],
+    "hv": lambda n, dt: [("hv", n, dt, HV_THETA)],
+    "implicit": lambda n, dt: [("implicit", n, dt, 1.0)],
+    "smooth": lambda n, dt: [("implicit", 2, dt * 0.5, 1.0), ("hv", n - 1, dt, 0.6)],
+}
+BATCH_ARGS = {
+    "douglas": lambda n, dt: dict(scheme="douglas", n_steps=n, dt=dt, theta=0.5),
+    "hv": lambda n, dt: dict(scheme="hv", n_steps=n, dt=dt, theta=HV_THETA),
+    "implicit": lambda n, dt: dict(scheme="douglas", n_steps=0, dt=dt, theta=0.5,
+                                   implicit_steps=n, implicit_dt_factor=1.0),
+    "smooth": lambda n, dt: dict(scheme="hv", n_steps=n - 1, dt=dt, theta=0.6,
+                                 implicit_steps=2, implicit_dt_factor=0.5),
+}
+
+
+def _rel(a, b):
+    return np.abs(a - b).max() / np.abs(b).max()
+
+
+@pytest.fixture(scope="module")
+def cuda():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from fd_adi_gb300 import _lib
+    _lib.load()
+    return torch.device("cuda", 0)
+
+
+@pytest.mark.parametrize("scheme", ["douglas", "hv", "implicit", "smooth"])
+def test_fused_batch_vs_golden(cuda, golden, scheme):
+    """Three parameter sets per scheme in one batch vs the reference outputs."""
+    from fd_adi_gb300.batch import HestonBatch
+    g = golden("solves")
+    keys = [str(k) for k in g["cases"]]
+    idx = [i for i, k in enumerate(keys) if k.split("_", 1)[1] == scheme]
+    params = [tuple(g["case_params"][i]) for i in idx]
+    mesh = (g["S"], g["v"])
+    b = HestonBatch(params, [mesh] * len(idx), **BATCH_ARGS[scheme](20, 0.01))
+    out = b.solve([g["V0"]] * len(idx))
+    for k, i in enumerate(idx):
+        ref = g[keys[i]]
+        assert _rel(out[k], ref) < 1e-11, keys[i]
+        r, kappa, theta, sigma, rho = params[k]
+        orc = O.heston_solve(g["S"], g["v"], r, kappa, theta, sigma, rho, g["V0"],
+                             SCHED[scheme](20, 0.01))
+        assert _rel(out[k], orc) < 1e-11, keys[i]
+
+
+def test_config1_price_and_grid(cuda, golden):
+    """150x150, nt=150: two implicit half-steps then Douglas theta=0.5."""
+    from fd_adi_gb300.batch import HestonBatch, payoff_grids
+    from fd_adi_gb300 import HestonOption
+    g = golden("config1")
+    opt = HestonOption(spot=100., strike=100., interest_rate=0.06, volatility=0.2, tenor=1.0,
+                       mean_reversion=1.0, mean_variance=0.04, vol_of_variance=0.2,
+                       correlation=0.0)
+    mesh = (g["S"], g["v"])
+    n, dt = 150, 1.0 / 150
+    b = HestonBatch([opt], [mesh], scheme="douglas", n_steps=n - 1, dt=dt, theta=0.5,
+                    implicit_steps=2, implicit_dt_factor=0.5)
+    V = b.solve(payoff_grids([opt], [mesh]))[0]
+    idx = tuple(g["idx"])
+    assert abs(V[idx] - g["price"]) <= 1e-10 * abs(g["price"])
+    assert np.abs(V - g["V"]).max() <= 1e-9
+    p = b.gather(b.pack([V]), b.flat_index()).cpu().numpy()[0]
+    assert p == V[idx]
+
+
+def test_config2_shape_vs_reference(cuda, golden):
+    """1024x512, rho=-0.7, sigma=0.5: 2 implicit half-steps + 3 HV steps."""
+    from fd_adi_gb300.batch import HestonBatch
+    g = golden("config2_short")
+    S, v = g["S"], g["v"]
+    V0 = np.maximum(S[:, None] - 100.0, 0) * np.ones((1, v.size))
+    dt = 1.0 / 1000
+    b = HestonBatch([(0.06, 1.0, 0.04, 0.5, -0.7)], [(S, v)], scheme="hv", n_steps=3, dt=dt,
+                    theta=HV_THETA, implicit_steps=2, implicit_dt_factor=0.5)
+    V = b.solve([V0])[0]
+    idx = tuple(g["idx"])
+    assert abs(V[idx] - g["price"]) <= 1e-10 * abs(g["price"])
+    assert np.abs(V[::16, ::8] - g["V_sub"]).max() <= 1e-9
+    assert abs(V.sum() - g["sum"]) <= 1e-10 * abs(g["sum"])
+    np.testing.assert_allclose(V.sum(axis=1), g["rowsum"], rtol=1e-11, atol=1e-9)
+
+
+def test_uneven_batch_vs_oracle(cuda):
+    """Sixteen options with different parameters and uneven grids in one launch chain."""
+    from fd_adi_gb300.batch import HestonBatch, payoff_grids
+    from fd_adi_gb300 import HestonOption, mesh
+    rng = np.random.RandomState(3)
+    opts, meshes = [], []
+    for k in range(16):
+        K = 100 * rng.uniform(0.7, 1.3)
+        v0 = rng.uniform(0.01, 0.16)
+        o = HestonOption(spot=100., strike=K, interest_rate=rng.uniform(0, 0.08), variance=v0,
+                         tenor=rng.uniform(0.1, 2.0), mean_reversion=rng.uniform(0.5, 5),
+                         mean_variance=rng.uniform(0.01, 0.16), vol_of_variance=rng.uniform(0.1, 1),
+                         correlation=rng.uniform(-0.9, 0))
+        nS = int(rng.choice(np.arange(32, 97, 16)))
+        nv = int(rng.choice(np.arange(16, 49, 8)))
+        opts.append(o)
+        meshes.append(mesh.heston_meshes(100., K, v0, nS, nv, 8 * K, 5.0))
+    n = 20
+    dts = [o.tenor / n for o in opts]
+    b = HestonBatch(opts, meshes, scheme="hv", n_steps=n - 1, dt=dts, theta=HV_THETA,
+                    implicit_steps=2, implicit_dt_factor=0.5)
+    V0 = payoff_grids(opts, meshes)
+    out = b.solve(V0)
+    ref = O.heston_batch(meshes, [o.params() for o in opts], V0,
+                         [[("implicit", 2, dt / 2, 1.0), ("hv", n - 1, dt, HV_THETA)] for dt in dts])
+    for k in range(16):
+        assert _rel(out[k], ref[k]) < 1e-11, k
+
+
+def test_graph_mode_matches_direct(cuda):
+    from fd_adi_gb300.batch import HestonBatch, payoff_grids
+    from fd_adi_gb300 import mesh
+    S, v = mesh.heston_meshes(100., 100., 0.04, 40, 20, 800., 5.)
+    p = (0.03, 2.0, 0.05, 0.6, -0.5)
+    kw = dict(scheme="hv", n_steps=9, dt=0.05, theta=HV_THETA, implicit_steps=2)
+    V0 = np.maximum(S[:, None] - 100.0, 0) * np.ones((1, v.size))
+    direct = HestonBatch([p], [(S, v)], **kw).solve([V0])[0]
+    gb = HestonBatch([p], [(S, v)], graph=True, **kw)
+    first = gb.solve([V0])[0]
+    again = gb.solve([V0])[0]   # replays the cached graph
+    np.testing.assert_array_equal(first, direct)
+    np.testing.assert_array_equal(again, direct)
+
+
+def test_barrier_option_vs_host_engine(cuda):
+    """Up-and-out: Dirichlet 0 at the barrier (heston.py:361-370); fused path vs
+    the per-operator path on the same mesh."""
+    from fd_adi_gb300 import HestonBarrierOption, HestonFiniteDifferenceEngine
+    o = HestonBarrierOption(spot=100., strike=100., interest_rate=0.03, variance=0.04, tenor=0.5,
+                            mean_reversion=1.5, mean_variance=0.04, vol_of_variance=0.3,
+                            correlation=-0.3, top=(False, 170.))
+    F = HestonFiniteDifferenceEngine(o, nspots=60, nvols=30, var_max=5.0)
+    G = HestonFiniteDifferenceEngine(o, nspots=60, nvols=30, var_max=5.0, fused=False)
+    a = F.solve_hundsdorferverwer(25, 0.02, theta=HV_THETA)
+    b_ = G.solve_hundsdorferverwer(25, 0.02, theta=HV_THETA)
+    assert _rel(a, b_) < 1e-11
+    assert np.all(a[-1] == 0)
+
+
+@pytest.mark.parametrize("scheme", ["douglas", "hv", "implicit", "smooth"])
+def test_plain_engine_vs_oracle(cuda, golden, scheme):
+    """The per-operator path (the reference's call sequence) vs the oracle."""
+    from fd_adi_gb300 import HestonOption, HestonFiniteDifferenceEngine, Grid
+    g = golden("solves")
+    r, kappa, theta, sigma, rho = 0.06, 1.0, 0.04, 0.5, -0.7
+    opt = HestonOption(spot=100., strike=100., interest_rate=r, variance=0.04, tenor=1.0,
+                       mean_reversion=kappa, mean_variance=theta, vol_of_variance=sigma,
+                       correlation=rho)
+    grid = Grid([g["S"], g["v"]], initializer=lambda *x: np.maximum(x[0] - 100., 0))
+    F = HestonFiniteDifferenceEngine(opt, grid=grid, fused=False)
+    fn = {"douglas": lambda: F.solve_douglas(20, 0.01, theta=0.5),
+          "hv": lambda: F.solve_hundsdorferverwer(20, 0.01, theta=HV_THETA),
+          "implicit": lambda: F.solve_implicit(20, 0.01),
+          "smooth": lambda: F.solve_smooth(20, 0.01, smoothing_steps=1)}[scheme]
+    out = fn()
+    ref = g["c1_" + scheme]
+    assert _rel(out, ref) < 1e-11
+
+
+def test_banded_operator_against_reference(cuda, golden):
+    """Operator-level API: apply/solve of the reference's operators."""
+    from fd_adi_gb300.construct import make_operators
+    from fd_adi_gb300.engine import heston_coefficients, heston_boundaries
+    g = golden("operators")
+    r, kappa, theta, sigma, rho = g["params"]
+    ops = make_operators([g["S"], g["v"]], heston_coefficients(r, kappa, theta, sigma, rho),
+                         heston_boundaries())
+    A0, A1, M = ops[0].to_gpu(), ops[1].to_gpu(), ops[(0, 1)].to_gpu()
+    X = g["X"]
+    assert _rel(A0.apply(X), g["apply0"]) < 1e-14
+    assert _rel(A1.apply(X), g["apply1"]) < 1e-14
+    assert _rel(M.apply(X), g["applyM"]) < 1e-13
+    Li0 = A0 * -0.01
+    Li0.add(1, inplace=True)
+    assert _rel(Li0.solve(X), g["solve0"]) < 1e-13
+    Li1 = A1 * (0.5 * -0.01)
+    Li1.add(1, inplace=True)
+    Li1.diagonalize()
+    assert Li1.bottom_fold_status == "FOLDED"
+    H = Li1.immigrate()
+    np.testing.assert_allclose(H.bottom_factors, g["Li1_bottom_factors"], rtol=1e-14)
+    assert _rel(Li1.solve(X), g["solve1_folded"]) < 1e-13
+    Li1.undiagonalize()
+    assert Li1.bottom_fold_status == "CAN_FOLD"
+    # the unfolded solve folds on the fly: same system
+    assert _rel(Li1.solve(X), g["solve1_folded"]) < 1e-13
+
+
+def test_for_vector_matches_host_construction(cuda, golden):
+    """Reference-GPU-style for_vector + scaling == the CPU construction."""
+    from fd_adi_gb300 import HestonOption, HestonFiniteDifferenceEngine, Grid
+    g = golden("operators")
+    r, kappa, theta, sigma, rho = g["params"]
+    opt = HestonOption(spot=100., strike=100., interest_rate=r, variance=0.04,
+                       mean_reversion=kappa, mean_variance=theta, vol_of_variance=sigma,
+                       correlation=rho)
+    grid = Grid([g["S"], g["v"]], initializer=lambda *x: np.maximum(x[0] - 100., 0))
+    F = HestonFiniteDifferenceEngine(opt, grid=grid, fused=False)
+    F.scale_and_combine_operators()
+    H0 = F.operators[0].immigrate()
+    H1 = F.operators[1].immigrate()
+    n = g["S"].size * g["v"].size
+    for H, key in ((H0, "A0"), (H1, "A1")):
+        rows = np.zeros((5, n))
+        for k, o in enumerate(H.D.offsets):
+            i = np.arange(max(0, -o), min(n, n - o))
+            rows[2 - o, i] = H.D.data[k][i + o]
+        np.testing.assert_allclose(rows, g[key], rtol=1e-15, atol=0)
+    np.testing.assert_allclose(F.operators[0].R.cpu().numpy(), g["R0"], rtol=1e-15)
+
+
+def test_blackscholes_engine(cuda, golden):
+    from fd_adi_gb300 import Option, Grid, BlackScholesFiniteDifferenceEngine
+    g = golden("blackscholes")
+    r, var, K = g["params"]
+    opt = Option(spot=100., strike=K, interest_rate=r, variance=var, tenor=1.0)
+    grid = Grid([g["S"]], initializer=lambda x: np.maximum(x - K, 0))
+    F = BlackScholesFiniteDifferenceEngine(opt, grid=grid)
+    n, dt = 200, 1.0 / 200
+    for name, fn in (("implicit", lambda: F.solve_implicit(n, dt)),
+                     ("douglas", lambda: F.solve_douglas(n, dt, theta=0.5)),
+                     ("hv", lambda: F.solve_hundsdorferverwer(n, dt, theta=0.5)),
+                     ("smooth", lambda: F.solve_smooth(n, dt, smoothing_steps=1))):
+        assert _rel(fn(), g[name]) < 1e-11, name
+
+
+def test_linearity_at_config2_size(cuda):
+    """Size-independent property at 1024x512: the scheme is linear in the
+    initial grid apart from the boundary residual, so
+    solve(a U + b W) - solve(0) = a (solve(U) - solve(0)) + b (solve(W) - solve(0))."""
+    from fd_adi_gb300.batch import HestonBatch
+    from fd_adi_gb300 import mesh
+    S, v = mesh.heston_meshes(100., 100., 0.04, 1024, 512, 800., 5.)
+    b = HestonBatch([(0.06, 1.0, 0.04, 0.5, -0.7)], [(S, v)], scheme="hv", n_steps=4,
+                    dt=0.001, theta=HV_THETA, implicit_steps=2)
+    rng = np.random.RandomState(0)
+    U = rng.rand(S.size, v.size)
+    W = rng.rand(S.size, v.size)
+    Z = np.zeros_like(U)
+    sU, sW, sZ, sM = b.solve([U])[0], b.solve([W])[0], b.solve([Z])[0], b.solve([2 * U - 3 * W])[0]
+    lhs = sM - sZ
+    rhs = 2 * (sU - sZ) - 3 * (sW - sZ)
+    assert np.abs(lhs - rhs).max() <= 1e-9 * np.abs(rhs).max()
