@@ -65,6 +65,14 @@ def workload(n_options, seed, nt=200):
                 nS=nS.astype(np.int32), nv=nv.astype(np.int32), nt=nt)
 
 
+def subset(w, idx):
+    out = dict(w)
+    for k, v in w.items():
+        if isinstance(v, np.ndarray):
+            out[k] = v[idx]
+    return out
+
+
 def _mesh_one(args):
     from fd_adi_gb300 import mesh
     S0, K, v0, nS, nv = args
@@ -297,8 +305,12 @@ def main():
     from fd_adi_gb300.batch import HestonBatch
     _lib.load()
 
-    # weak scaling: every rank prices its own seeded batch of args.options
-    w = workload(args.options, args.seed + rank)
+    # weak scaling: the seeded workload has args.options options per rank and
+    # is partitioned across ranks by work (no data-path collective)
+    from fd_adi_gb300.shard import shard_of
+    w_all = workload(args.options * world, args.seed)
+    mine = shard_of(w_all["nS"].astype(np.int64) * w_all["nv"], rank, world)
+    w = subset(w_all, mine)
     meshes = meshes_for(w)
     params = params_of(w)
     nt = w["nt"]
@@ -368,7 +380,7 @@ def main():
     torch.cuda.synchronize()
     ms_e2e = timed(step_e2e, max(1, args.steps))
 
-    n_total = args.options * world
+    n_total = len(w_all["K"])
     value = n_total / (ms * 1e-3)
     e2e_value = n_total / (ms_e2e * 1e-3)
     h2d = sum(t.numel() * t.element_size() for t in (h_spots, h_vars, h_params, h_dt, h_V0))
