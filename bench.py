@@ -214,6 +214,68 @@ def stage_times(batch, V, torch):
     return {k: (acc[k] / cnt[k], cnt[k], acc[k]) for k in acc}
 
 
+def plain_vs_batched(torch, n_batch=2048):
+    """Config 1 (150x150, nt=150: two implicit half-steps then Douglas 0.5):
+    options/s of the per-operator engine (the reference's per-step call
+    sequence, one option per launch chain) vs the fused batched engine."""
+    from fd_adi_gb300 import HestonOption, HestonFiniteDifferenceEngine, mesh
+    from fd_adi_gb300.batch import HestonBatch
+    n, dt = 150, 1.0 / 150
+    opt = HestonOption(spot=100., strike=100., interest_rate=0.06, volatility=0.2, tenor=1.0,
+                       mean_reversion=1.0, mean_variance=0.04, vol_of_variance=0.2,
+                       correlation=0.0)
+    S, v = mesh.heston_meshes(100., 100., 0.04, 150, 150, 800., 5.)
+    grid_host = np.maximum(S[:, None] - 100., 0) * np.ones((1, v.size))
+
+    def plain_once():
+        from fd_adi_gb300 import Grid
+        F = HestonFiniteDifferenceEngine(opt, grid=Grid([S.copy(), v.copy()],
+                                                        initializer=lambda *x: np.maximum(
+                                                            x[0] - 100., 0)), fused=False)
+        V = F._initial(None)
+        F.solve_implicit_(2, dt * 0.5, V)
+        F.solve_douglas_(n - 1, dt, V, 0.5)
+        return float(V[F.idx].item())
+
+    plain_once()
+    torch.cuda.synchronize()
+    reps = 3
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        p_plain = plain_once()
+    torch.cuda.synchronize()
+    plain = reps / (time.perf_counter() - t0)
+    b = HestonBatch([opt] * n_batch, [(S, v)] * n_batch, scheme="douglas", n_steps=n - 1, dt=dt,
+                    theta=0.5, implicit_steps=2, implicit_dt_factor=0.5, graph=True)
+    V0 = b.pack([grid_host] * n_batch)
+    V = torch.empty_like(V0)
+    idx = b.flat_index()
+    out = torch.empty(n_batch, dtype=torch.float64, device="cuda")
+
+    def batched_once():
+        with torch.cuda.stream(b.stream):
+            b._prepare()
+            V.copy_(V0, non_blocking=True)
+            b.run(V)
+            b.gather(V, idx, out)
+
+    batched_once()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(b.stream)
+    for _ in range(reps):
+        batched_once()
+    e1.record(b.stream)
+    torch.cuda.synchronize()
+    batched = reps * n_batch / (e0.elapsed_time(e1) * 1e-3)
+    p_batch = float(out[0].item())
+    return {"config": "150x150, nt=150, 2 implicit half-steps + Douglas theta=0.5",
+            "plain_options_per_s": plain, "batched_options_per_s": batched,
+            "ratio": batched / plain, "batch": n_batch,
+            "price_plain": p_plain, "price_batched": p_batch,
+            "price_rel_diff": abs(p_plain - p_batch) / abs(p_plain)}
+
+
 def cpu_baseline(w, n_sample, kind_pref="port"):
     """Oracle (C restatement, OpenMP over options) or the compat-built
     reference on this host's cores, on the first n_sample options."""
@@ -325,7 +387,7 @@ def main():
     h_params = batch.params.cpu().pin_memory()
     h_dt = batch.dt.cpu().pin_memory()
     h_V0 = V0_dev.cpu().pin_memory()
-    flat_idx = batch.flat_index()
+    flat_idx = batch.flat_index([(w["S0"], v0) for v0 in w["v0"]])
     prices = torch.empty(batch.n, dtype=torch.float64, device="cuda")
     h_prices = torch.empty(batch.n, dtype=torch.float64).pin_memory()
     stream = batch.stream
@@ -417,8 +479,9 @@ def main():
                              "flops_per_point": STAGE_FLOPS[dom]},
                "stage_ms": {k: round(v[0], 4) for k, v in st.items()},
                "clocks": clk}
+        out["cpu_baseline"] = cpu_baseline(w, args.cpu_sample)
         if not args.no_extras:
-            out["cpu_baseline"] = cpu_baseline(w, args.cpu_sample)
+            out["plain_vs_batched"] = plain_vs_batched(torch)
     if world > 1:
         dist.barrier()
         dist.destroy_process_group()

@@ -141,18 +141,21 @@ class HestonBatch(object):
         self.run(V)
         return self.unpack(V)
 
-    def flat_index(self, meshes=None, points=None):
+    def flat_index(self, points=None):
         """Arena index of each option's (spot, variance) grid point, by the
-        reference's rounded bisection (FiniteDifferenceEngineGPU.pyx:727-734)."""
+        reference's rounded bisection (FiniteDifferenceEngineGPU.pyx:727-734).
+        points: per-option (spot, variance); default: the options' own."""
+        if points is None:
+            points = [(o.spot, o.variance.value) for o in self.options]
         idx = np.zeros(self.n, dtype=np.int64)
         spots = self.spots.cpu().numpy()
         vars_ = self.vars.cpu().numpy()
         s0 = np.concatenate([[0], np.cumsum(self.n0)])
         v0 = np.concatenate([[0], np.cumsum(self.n1)])
-        for k, o in enumerate(self.options):
+        for k, (spot, variance) in enumerate(points):
             S = spots[s0[k]:s0[k + 1]]
             v = vars_[v0[k]:v0[k + 1]]
-            i, j = _mesh.price_index(S, v, o.spot, o.variance.value)
+            i, j = _mesh.price_index(S, v, spot, variance)
             idx[k] = self.p_off[k] + i * self.n1[k] + j
         return torch.as_tensor(idx, device=self.device)
 
