@@ -14,6 +14,7 @@ FOLD_CODES = {"CANNOT_FOLD": 0, "CAN_FOLD": 1, "FOLDED": 2}
 FOLD_NAMES = {v: k for k, v in FOLD_CODES.items()}
 SCHEME_IMPLICIT, SCHEME_DOUGLAS, SCHEME_HV = 0, 1, 2
 HESTON_DROP_ZERO_MIXED, HESTON_GRAPH = 1, 2
+NOALLOC_MAX_ROWS = 1 << 20
 
 c_double_p = ctypes.POINTER(ctypes.c_double)
 c_int32_p = ctypes.POINTER(ctypes.c_int32)
@@ -61,6 +62,8 @@ SIGNATURES = {
                                        ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p]),
     "fdadi_tri_solve": (ctypes.c_int, [ctypes.POINTER(Tri), ctypes.c_void_p, ctypes.c_int64,
                                        ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p]),
+    "fdadi_tri_solve_noalloc": (ctypes.c_int, [ctypes.POINTER(Tri), ctypes.c_void_p,
+                                               ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p]),
     "fdadi_tri_scale": (ctypes.c_int, [ctypes.POINTER(Tri), ctypes.c_void_p, ctypes.c_double,
                                        ctypes.c_void_p]),
     "fdadi_tri_add_scalar": (ctypes.c_int, [ctypes.POINTER(Tri), ctypes.c_double,

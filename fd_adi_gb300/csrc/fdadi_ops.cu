@@ -9,6 +9,8 @@
 #include <stdarg.h>
 #include <string.h>
 
+#include <mutex>
+
 #include "fdadi_internal.cuh"
 
 namespace fdadi {
@@ -447,3 +449,65 @@ int fdadi_axpby(double *y, const double *x, double a, double b, int64_t n, void 
 }
 
 }  // extern "C"
+
+// ---- tridiagonal solve without caller scratch -----------------------------
+//
+// Some callers cannot allocate device memory themselves: a host application
+// that hands out every byte of device memory from its own fixed pool and
+// forbids components to call cudaMalloc, or a latency-critical pricing loop
+// where cudaMalloc/cudaFree would synchronize the whole device between
+// requests. fdadi_tri_solve asks them for an operator-sized scratch buffer;
+// fdadi_tri_solve_noalloc instead uses the library's own scratch below, a
+// fixed array that every device which loads the library holds until the
+// process exits.
+//
+// The array is one per device and shared by every call: calls whose kernels
+// overlap on the GPU (different streams, different host threads) race on it,
+// so the caller must order them. The solve writes every scratch element it
+// reads before reading it, so the contents a previous call left behind never
+// matter and nothing needs clearing.
+
+namespace fdadi {
+
+// FDADI_NOALLOC_MAX_ROWS doubles (8 MiB) per device.
+static __device__ __align__(256) double g_noalloc_scratch[FDADI_NOALLOC_MAX_ROWS];
+
+static std::mutex g_noalloc_mu;
+static double *g_noalloc_addr[64] = {nullptr};
+
+// Device address of g_noalloc_scratch on the current device, looked up once
+// per device (host code cannot use the symbol itself as a pointer).
+static int noalloc_scratch(double **out) {
+    int dev = 0;
+    FDADI_CUDA(cudaGetDevice(&dev));
+    FDADI_REQUIRE(dev >= 0 && dev < 64, "device ordinal %d out of range", dev);
+    std::lock_guard<std::mutex> g(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void *p = nullptr;
+        FDADI_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        g_noalloc_addr[dev] = static_cast<double *>(p);
+    }
+    *out = g_noalloc_addr[dev];
+    return FDADI_OK;
+}
+
+}  // namespace fdadi
+
+extern "C" int fdadi_tri_solve_noalloc(const fdadi_tri_t *op, double *x, int64_t n0, int64_t n1,
+                                       void *stream) {
+    int rc = check_tri(op, n0, n1, true);
+    if (rc) return rc;
+    FDADI_REQUIRE(x, "null grid pointer");
+    FDADI_REQUIRE(op->operator_rows <= FDADI_NOALLOC_MAX_ROWS,
+                  "fdadi_tri_solve_noalloc: %lld operator rows exceed the library scratch of %d "
+                  "rows; use fdadi_tri_solve with caller scratch",
+                  (long long)op->operator_rows, (int)FDADI_NOALLOC_MAX_ROWS);
+    double *scratch = nullptr;
+    rc = noalloc_scratch(&scratch);
+    if (rc) return rc;
+    const int threads = 128;
+    tri_solve_kernel<<<grid_for(op->blocks, threads), threads, 0, as_stream(stream)>>>(*op, x, n1,
+                                                                                      scratch);
+    FDADI_CHECK_LAUNCH();
+    return FDADI_OK;
+}

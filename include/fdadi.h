@@ -91,6 +91,20 @@ int fdadi_tri_apply(const fdadi_tri_t *op, const double *x, double *y,
 int fdadi_tri_solve(const fdadi_tri_t *op, double *x, int64_t n0, int64_t n1,
                     double *scratch, void *stream);
 
+/* Same solve as fdadi_tri_solve for callers that cannot allocate device
+ * memory (a host that owns all device memory in its own pool, or a latency-
+ * critical loop that must not let cudaMalloc/cudaFree synchronize the
+ * device). No counterpart in the reference. The scratch is the library's own
+ * static device array of FDADI_NOALLOC_MAX_ROWS doubles (8 MiB), held by
+ * every device that loads the library until the process exits; operators with
+ * more rows are rejected (FDADI_E_ARG). The first call on a device looks up
+ * the array's device address (cudaGetSymbolAddress) and caches it; make that
+ * first call before any stream capture. All calls share the array, so calls
+ * whose kernels overlap on the GPU race: order them. */
+#define FDADI_NOALLOC_MAX_ROWS (1 << 20)
+int fdadi_tri_solve_noalloc(const fdadi_tri_t *op, double *x, int64_t n0, int64_t n1,
+                            void *stream);
+
 /* Row r of every diagonal, R and the fold extras scaled by vec[r]; Dirichlet
  * rows are left alone. Replaces vectorized_scale
  * (_TriBandedOperatorGPU.cu:1012-1105). If vec is NULL, `scalar` is used for
