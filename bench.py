@@ -34,13 +34,18 @@ UNIT = "options/s"
 HV_THETA = 0.5 + np.sqrt(3.0) / 6.0
 
 # Algorithmic state traffic (bytes per grid point) and FP64 work (flops per
-# grid point, an FMA counts 2) of one launch of each stage kernel.
+# grid point, an FMA counts 2) of one launch of each stage kernel. State
+# traffic counts the stage's input and output grids once (operator
+# coefficients, which stream at the same time, are not counted). Flops: spot
+# and variance applies 3 FMA each, the mixed term 3 FMA for the shared row
+# sums (x 10/8 for the tile halo) + 3 FMA + 1 MUL, the scheme combination
+# 4-6; Thomas solves FMA + MUL forward and FMA backward (+1 for x - T).
 STAGE_BYTES = {"explicit_hv0": 32, "explicit_hv3": 40, "spot_solve": 24, "var_solve_y2": 16,
                "var_solve_v": 16, "explicit_implicit": 16, "var_solve_implicit": 16,
                "spot_solve_implicit": 16}
-STAGE_FLOPS = {"explicit_hv0": 40, "explicit_hv3": 60, "spot_solve": 7, "var_solve_y2": 6,
-               "var_solve_v": 6, "explicit_implicit": 16, "var_solve_implicit": 7,
-               "spot_solve_implicit": 7}
+STAGE_FLOPS = {"explicit_hv0": 33.5, "explicit_hv3": 35.5, "spot_solve": 6, "var_solve_y2": 5,
+               "var_solve_v": 5, "explicit_implicit": 15.5, "var_solve_implicit": 5,
+               "spot_solve_implicit": 5}
 
 
 def workload(n_options, seed, nt=200):

@@ -2,24 +2,35 @@
 //
 // A batch of options with independent (uneven) grids lives in one packed
 // arena: option k owns points [p_off[k], p_off[k] + n0*n1) of every per-point
-// array, rows [s_off[k], s_off[k] + n0) of every per-spot-index array and
-// columns [v_off[k], v_off[k] + n1) of every per-variance-index array. Each
-// time step is a short chain of launches over the whole batch:
+// array (row-major, variance contiguous), rows [s_off[k], s_off[k] + n0) of
+// every per-spot-index array and columns [v_off[k], v_off[k] + n1) of every
+// per-variance-index array. Each time step is a short chain of launches over
+// the whole batch:
 //
-//   explicit stage  -- one thread per grid point: the three operator applies
-//                      of F(V) (spot, variance, mixed) fused with the scheme's
-//                      combination, writing the next right-hand side;
-//   spot solve      -- one thread per spot line (grid column); adjacent
-//                      threads read adjacent columns, so the strided
-//                      direction is coalesced without a transpose;
-//   variance solve  -- one thread per variance line (grid row).
+//   explicit stage  -- 8x32-point tiles staged in shared memory with a halo:
+//                      the spot, variance and mixed applies of F(V) fused
+//                      with the scheme's combination; the mixed stencil's
+//                      row sums are formed once per tile row and shared;
+//   spot solve      -- one thread per grid column walking the strided
+//                      direction; adjacent threads read adjacent columns, so
+//                      every access is coalesced without a transpose;
+//   variance solve  -- one warp per 32 grid rows: 32x32 chunks pass through
+//                      a padded shared tile so global loads and stores are
+//                      coalesced while each lane runs its row's recurrence.
 //
-// Line solves use Thomas factors precomputed once per (dt, theta): the
-// operators are time independent (FiniteDifferenceEngineGPU.pyx:163-167), so
-// every step costs two FMAs and a multiply per point per solve and no
-// division. Operators are built on the device with the reference's
-// arithmetic order (explicitly rounded intrinsics, no FMA contraction), so
-// they equal the reference CPU engine's bit for bit.
+// GB300 executes FP64 at ~1 TFLOP/s against ~6.8 TB/s of HBM, so the kernels
+// are built to minimise FP64 instructions first: Thomas factors are
+// precomputed once per (dt, theta) (the operators are time independent,
+// FiniteDifferenceEngineGPU.pyx:163-167), each solve costs two FMAs and a
+// multiply per point, the HV corrector reuses F(V) from the predictor, and the
+// mixed stencil is factored. The variance operator of the Heston PDE is the
+// same on every spot row with S > 0 (its coefficients kappa(theta - v) and
+// sigma^2 v / 2 do not depend on S, heston.py:309-322), so its coefficients
+// and Thomas factors are stored once per option as 1-D arrays.
+//
+// Operators are built on the device with the reference's arithmetic order
+// (explicitly rounded intrinsics, no FMA contraction), so they equal the
+// reference CPU engine's bit for bit.
 #include <algorithm>
 #include <mutex>
 #include <unordered_map>
@@ -34,26 +45,45 @@ namespace fdadi {
 #define SUB(a, b) __dsub_rn((a), (b))
 #define DIV(a, b) __ddiv_rn((a), (b))
 
-enum : int { OPT_S_LOW_DIR = 1, OPT_S_HIGH_DIR = 2, OPT_MIXED = 4 };
+enum : int { OPT_S_LOW_DIR = 1, OPT_S_HIGH_DIR = 2, OPT_MIXED = 4, OPT_ROW0_ZERO = 8 };
 
-constexpr int EXPL_TILE = 256;
+constexpr int TI = 8;                 // explicit tile rows
+constexpr int TJ = 32;                // explicit tile columns
+constexpr int EXPL_THREADS = TI * TJ;
+constexpr int XR = TI + 2;            // staged rows (one-row halo above and below)
+constexpr int XC = TJ + 3;            // staged columns (two on the left, one on the right)
+constexpr int XCP = 36;               // padded row pitch of the staged tile
 constexpr int SOLVE_THREADS = 128;
+constexpr int VS_WARPS = 4;           // warps per variance-solve block
+constexpr int VS_PITCH = 33;          // padded pitch of the 32x32 variance tile
 
 // Device view of a prepared workspace.
 struct Arena {
     int n_opt;
-    int64_t P, SS, SV;        // total points, total spot indices, total variance indices
+    int64_t P, SS, SV;         // total points, total spot indices, total variance indices
     // tables
     const int *n0, *n1, *oflags;
     const int64_t *p_off, *s_off, *v_off;
-    const int *lineS, *lineV;  // option of each spot line (grid column) / variance line (grid row)
-    const int2 *tiles;         // (option, first point) of each explicit tile
+    const int *lineS;          // option of each spot line (grid column)
+    const int4 *tiles;         // explicit tiles: (option, i0, j0, -)
+    const int4 *vtasks;        // variance-solve tasks: (option, i0, rows, -)
     // main plan (dt, theta)
-    double *F0, *R0, *F1, *R1, *F1x, *cM, *w0, *w1, *LS, *LV, *foldV, *dirS;
-    // implicit plan (dt/2, theta = 1, residual kept)
-    double *cMi, *RSi, *RVi, *LSi, *LVi, *foldVi;
+    double *F0;                // [3P] spot operator rows (sub, mid, sup) * dt; Dirichlet rows identity
+    double *cM;                // [P] mixed coefficient rho sigma S v * dt
+    double *w0, *w1;           // [3 SS], [3 SV] centred first-derivative weights
+    double *LS;                // [3P] Thomas factors (a, 1/m, c') of 1 - theta dt A0
+    double *R0top;             // [SV] spot residual on the S_max row * dt
+    double *F1v;               // [3 SV] variance operator rows on S > 0 * dt
+    double *F1x;               // [n_opt] its A[n1-1, n1-3] * dt
+    double *F1z;               // [n_opt] variance operator on S = 0 (diagonal) * dt
+    double *LVv;               // [3 SV] factors of 1 - theta dt A1 on S > 0, bottom folded
+    double *foldV;             // [n_opt] bottom fold factor of that operator
+    double *LVz;               // [n_opt] 1/diagonal of 1 - theta dt A1 on S = 0
+    double *dirS;              // [2 SV] Dirichlet values of the spot lines (low, high)
+    // implicit plan (dt * factor, theta = 1, residual kept)
+    double *cMi, *RSi, *LSi, *LVvi, *foldVi, *LVzi;
     // stage buffers
-    double *Y0, *W, *T, *Y2;
+    double *FV, *W, *T, *Y2;
     const double *theta;       // [n_opt]
 };
 
@@ -164,6 +194,7 @@ struct BuildArgs {
     double theta;
     double dt_factor;  // implicit step = dt * dt_factor
     int smoothing;     // nonzero: build the implicit plan too
+    int drop_zero_mixed;
 };
 
 __device__ __forceinline__ void opt_params(const BuildArgs &a, int o, double &r, double &kappa,
@@ -172,76 +203,127 @@ __device__ __forceinline__ void opt_params(const BuildArgs &a, int o, double &r,
     r = p[0]; kappa = p[1]; th = p[2]; sigma = p[3]; rho = p[4];
 }
 
-// Per point: scaled explicit operators (Firsts = A * dt), mixed coefficient,
-// residuals of the implicit plan; per line/index: stencil weights, extras,
-// Dirichlet values.
-__global__ void build_points_kernel(Arena A, BuildArgs a) {
-    const int2 t = A.tiles[blockIdx.x];
-    const int o = t.x;
-    const int n0 = A.n0[o], n1 = A.n1[o];
-    const int64_t N = (int64_t)n0 * n1;
-    const int64_t pl = (int64_t)t.y + threadIdx.x;
-    if (pl >= N) return;
-    const int i = (int)(pl / n1), j = (int)(pl - (int64_t)i * n1);
-    const int64_t p = A.p_off[o] + pl, P = A.P;
+// Thomas factors (a_k, 1/m_k, c'_k) of one line with rows (sub, mid, sup):
+// m_0 = mid_0, m_k = mid_k - sub_k c'_{k-1}, c'_k = sup_k / m_k; stored at
+// L[q], L[stride + q], L[2 stride + q].
+struct Thomas {
+    double cp = 0.0;
+    __device__ __forceinline__ void row(double *L, int64_t stride, int64_t q, double sub, double mid,
+                                        double sup, bool first) {
+        const double m = first ? mid : mid - sub * cp;
+        const double inv = 1.0 / m;
+        cp = sup * inv;
+        L[q] = sub;
+        L[stride + q] = inv;
+        L[2 * stride + q] = cp;
+    }
+};
+
+// Per option: flags, the 1-D variance operator on S > 0 and S = 0 and the
+// Thomas factors of 1 - theta dt A1 (bottom folded, BandedOperator.pyx:223-256)
+// for the main and implicit plans.
+__device__ void var_factors(const Arena &A, int o, const double *v, int n1, double r, float half_r,
+                            double kappa, double th, double sigma, double scale, double *L,
+                            double *fold, double *zinv) {
+    const int64_t vo = A.v_off[o];
+    const Row3 a2 = var_row(v, n1, n1 - 2, 1.0, r, half_r, kappa, th, sigma);
+    const Row3 a1 = var_row(v, n1, n1 - 1, 1.0, r, half_r, kappa, th, sigma);
+    const double an1 = MUL(a2.sub, scale), bn1 = ADD(MUL(a2.mid, scale), 1.0),
+                 cn1 = MUL(a2.sup, scale);
+    const double zn = MUL(a1.ext, scale);
+    double an = MUL(a1.sub, scale), bn = ADD(MUL(a1.mid, scale), 1.0);
+    const double f = an1 != 0.0 ? DIV(-zn, an1) : 0.0;
+    an = ADD(an, MUL(bn1, f));
+    bn = ADD(bn, MUL(cn1, f));
+    fold[o] = f;
+    Thomas t;
+    for (int j = 0; j < n1 - 1; ++j) {
+        const Row3 w = var_row(v, n1, j, 1.0, r, half_r, kappa, th, sigma);
+        t.row(L, A.SV, vo + j, MUL(w.sub, scale), ADD(MUL(w.mid, scale), 1.0), MUL(w.sup, scale),
+              j == 0);
+    }
+    t.row(L, A.SV, vo + n1 - 1, an, bn, 0.0, false);
+    // S = 0: A1 is (-r/2) I (both variance coefficients vanish there)
+    const Row3 z = var_row(v, n1, 0, 0.0, r, half_r, kappa, th, sigma);
+    *zinv = 1.0 / ADD(MUL(z.mid, scale), 1.0);
+}
+
+__global__ void build_options_kernel(Arena A, BuildArgs a) {
+    const int o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= A.n_opt) return;
+    const int n1 = A.n1[o];
     const double *S = a.spots + A.s_off[o], *v = a.vars + A.v_off[o];
     double r, kappa, th, sigma, rho;
     opt_params(a, o, r, kappa, th, sigma, rho);
     const float half_r = (float)(-r / 2.0);   // add_scalar takes a C float (BandedOperator.pxd:32)
+    const double dt = a.dt[o];
+    const bool barrier = a.barrier && a.barrier[o];
+    int fl = OPT_S_LOW_DIR;
+    if (barrier) fl |= OPT_S_HIGH_DIR;
+    if (!(a.drop_zero_mixed && rho == 0.0)) fl |= OPT_MIXED;
+    if (S[0] == 0.0) fl |= OPT_ROW0_ZERO;
+    const_cast<int *>(A.oflags)[o] = fl;
+    const Row3 xb = var_row(v, n1, n1 - 1, 1.0, r, half_r, kappa, th, sigma);
+    A.F1x[o] = MUL(xb.ext, dt);
+    const Row3 z = var_row(v, n1, 0, 0.0, r, half_r, kappa, th, sigma);
+    A.F1z[o] = MUL(z.mid, dt);
+    var_factors(A, o, v, n1, r, half_r, kappa, th, sigma, MUL(a.theta, -dt), A.LVv, A.foldV,
+                &A.LVz[o]);
+    if (a.smoothing)
+        var_factors(A, o, v, n1, r, half_r, kappa, th, sigma, -MUL(dt, a.dt_factor), A.LVvi,
+                    A.foldVi, &A.LVzi[o]);
+}
+
+// Per point: scaled spot operator rows (Firsts = A0 * dt, Dirichlet rows
+// unscaled, BandedOperator.pyx:771-779) and mixed coefficients; per spot
+// index: stencil weights; per variance index: stencil weights, the variance
+// operator rows, the S_max residual and the Dirichlet values.
+__global__ void build_points_kernel(Arena A, BuildArgs a) {
+    const int4 t = A.tiles[blockIdx.x];
+    const int o = t.x, n0 = A.n0[o], n1 = A.n1[o];
+    const int i = t.y + threadIdx.x / TJ, j = t.z + threadIdx.x % TJ;
+    if (i >= n0 || j >= n1) return;
+    const int64_t p = A.p_off[o] + (int64_t)i * n1 + j, P = A.P;
+    const double *S = a.spots + A.s_off[o], *v = a.vars + A.v_off[o];
+    double r, kappa, th, sigma, rho;
+    opt_params(a, o, r, kappa, th, sigma, rho);
+    const float half_r = (float)(-r / 2.0);
     const bool barrier = a.barrier && a.barrier[o];
     const double dt = a.dt[o];
+    const double dti = MUL(dt, a.dt_factor);
 
     const Row3 s = spot_row(S, n0, i, v[j], r, half_r, barrier);
-    if (s.dirichlet) {  // Dirichlet rows are not scaled (BandedOperator.pyx:771-779)
-        A.F0[p] = 0.0; A.F0[P + p] = 1.0; A.F0[2 * P + p] = 0.0; A.R0[p] = s.R;
+    if (s.dirichlet) {
+        A.F0[p] = 0.0; A.F0[P + p] = 1.0; A.F0[2 * P + p] = 0.0;
     } else {
         A.F0[p] = MUL(s.sub, dt); A.F0[P + p] = MUL(s.mid, dt); A.F0[2 * P + p] = MUL(s.sup, dt);
-        A.R0[p] = MUL(s.R, dt);
     }
-    const Row3 w = var_row(v, n1, j, S[i], r, half_r, kappa, th, sigma);
-    A.F1[p] = MUL(w.sub, dt); A.F1[P + p] = MUL(w.mid, dt); A.F1[2 * P + p] = MUL(w.sup, dt);
-    A.R1[p] = MUL(w.R, dt);
-    if (j == n1 - 1) A.F1x[A.s_off[o] + i] = MUL(w.ext, dt);
     const double c = MUL(MUL(MUL(rho, sigma), S[i]), v[j]);
     A.cM[p] = MUL(c, dt);
-    if (a.smoothing) {
-        const double dti = MUL(dt, a.dt_factor);
-        A.cMi[p] = MUL(c, dti);
-        A.RSi[p] = s.dirichlet ? s.R : MUL(s.R, -dti);
-        A.RVi[p] = MUL(w.R, -dti);
-    }
-    if (j == 0) {  // spot stencil weights (centred first derivative, rows 0 and n0-1 zero)
+    if (a.smoothing) A.cMi[p] = MUL(c, dti);
+    if (j == 0) {
         double sb = 0.0, md = 0.0, sp = 0.0;
         if (i > 0 && i < n0 - 1) centre(S, i, 1, sb, md, sp);
         const int64_t q = A.s_off[o] + i;
         A.w0[q] = sb; A.w0[A.SS + q] = md; A.w0[2 * A.SS + q] = sp;
     }
-    if (i == 0) {  // variance stencil weights; Dirichlet values of the spot lines (U = 0)
+    if (i == 0) {
+        const int64_t q = A.v_off[o] + j;
         double sb = 0.0, md = 0.0, sp = 0.0;
         if (j > 0 && j < n1 - 1) centre(v, j, 1, sb, md, sp);
-        const int64_t q = A.v_off[o] + j;
         A.w1[q] = sb; A.w1[A.SV + q] = md; A.w1[2 * A.SV + q] = sp;
         A.dirS[q] = 0.0;
         A.dirS[A.SV + q] = 0.0;
+        const Row3 top = spot_row(S, n0, n0 - 1, v[j], r, half_r, barrier);
+        A.R0top[q] = top.dirichlet ? top.R : MUL(top.R, dt);
+        if (a.smoothing) A.RSi[q] = top.dirichlet ? top.R : MUL(top.R, -dti);
+        const Row3 w = var_row(v, n1, j, 1.0, r, half_r, kappa, th, sigma);
+        A.F1v[q] = MUL(w.sub, dt); A.F1v[A.SV + q] = MUL(w.mid, dt);
+        A.F1v[2 * A.SV + q] = MUL(w.sup, dt);
     }
 }
 
-// Thomas factors (a_k, 1/m_k, c'_k) of one line with rows (sub, mid, sup):
-// m_0 = mid_0, m_k = mid_k - sub_k c'_{k-1}, c'_k = sup_k / m_k.
-struct Thomas {
-    double cp = 0.0;
-    __device__ __forceinline__ void row(double *L, int64_t P, int64_t p, double sub, double mid,
-                                        double sup, bool first) {
-        const double m = first ? mid : mid - sub * cp;
-        const double inv = 1.0 / m;
-        cp = sup * inv;
-        L[p] = sub;
-        L[P + p] = inv;
-        L[2 * P + p] = cp;
-    }
-};
-
-// Spot lines: factors of Li0 = 1 - theta dt A0 (main) and 1 - dt/2 A0 (implicit).
+// Spot lines: factors of Li0 = 1 - theta dt A0 (main) and 1 - dt f A0 (implicit).
 __global__ void build_spot_lines_kernel(Arena A, BuildArgs a) {
     const int64_t line = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (line >= A.SV) return;
@@ -270,141 +352,100 @@ __global__ void build_spot_lines_kernel(Arena A, BuildArgs a) {
     }
 }
 
-// Variance lines: Li1 folded at the bottom (BandedOperator.pyx:223-256) and
-// factorised; the fold factor is kept for the right-hand side.
-__device__ void var_line_factor(const Arena &A, int o, int i, const double *v, int n1, double Si,
-                                double r, float half_r, double kappa, double th, double sigma,
-                                double scale, double *L, double *fold) {
-    const int64_t base = A.p_off[o] + (int64_t)i * n1;
-    // rows n1-2 and n1-1 are needed before the last row is factorised
-    const Row3 a2 = var_row(v, n1, n1 - 2, Si, r, half_r, kappa, th, sigma);
-    const Row3 a1 = var_row(v, n1, n1 - 1, Si, r, half_r, kappa, th, sigma);
-    const double an1 = MUL(a2.sub, scale), bn1 = ADD(MUL(a2.mid, scale), 1.0),
-                 cn1 = MUL(a2.sup, scale);
-    const double zn = MUL(a1.ext, scale);
-    double an = MUL(a1.sub, scale), bn = ADD(MUL(a1.mid, scale), 1.0);
-    const double f = an1 != 0.0 ? DIV(-zn, an1) : 0.0;
-    an = ADD(an, MUL(bn1, f));
-    bn = ADD(bn, MUL(cn1, f));
-    fold[A.s_off[o] + i] = f;
-    Thomas t;
-    for (int j = 0; j < n1 - 1; ++j) {
-        const Row3 w = var_row(v, n1, j, Si, r, half_r, kappa, th, sigma);
-        t.row(L, A.P, base + j, MUL(w.sub, scale), ADD(MUL(w.mid, scale), 1.0), MUL(w.sup, scale),
-              j == 0);
-    }
-    t.row(L, A.P, base + n1 - 1, an, bn, 0.0, false);
-}
-
-__global__ void build_var_lines_kernel(Arena A, BuildArgs a) {
-    const int64_t line = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (line >= A.SS) return;
-    const int o = A.lineV[line];
-    const int n1 = A.n1[o];
-    const int i = (int)(line - A.s_off[o]);
-    const double *S = a.spots + A.s_off[o], *v = a.vars + A.v_off[o];
-    double r, kappa, th, sigma, rho;
-    opt_params(a, o, r, kappa, th, sigma, rho);
-    const float half_r = (float)(-r / 2.0);
-    const double dt = a.dt[o];
-    var_line_factor(A, o, i, v, n1, S[i], r, half_r, kappa, th, sigma, MUL(a.theta, -dt), A.LV,
-                    A.foldV);
-    if (a.smoothing)
-        var_line_factor(A, o, i, v, n1, S[i], r, half_r, kappa, th, sigma, -MUL(dt, a.dt_factor),
-                        A.LVi, A.foldVi);
-}
-
 // ---- stage kernels --------------------------------------------------------
 
 enum : int { ST_DOUGLAS = 0, ST_HV0 = 1, ST_HV3 = 2, ST_IMPLICIT = 3 };
 
-// Grid-point accessor with the spot operator's forced Dirichlet rows.
-struct OptView {
-    int n0, n1, flags;
-    int64_t p0;      // first point of the option
-    int64_t sv;      // v_off: first spot-line index
-    int64_t ss;      // s_off
-};
-
+// One 8x32 tile of one option. X (the operand of the applies: V, or Y2 in
+// the HV corrector) is staged with a halo of one row above and below, two
+// columns on the left (the A[n1-1, n1-3] corner) and one on the right.
 template <int MODE>
-__global__ void __launch_bounds__(EXPL_TILE) explicit_kernel(Arena A, const double *__restrict__ V) {
-    const int2 t = A.tiles[blockIdx.x];
-    const int o = t.x;
+__global__ void __launch_bounds__(EXPL_THREADS) explicit_kernel(Arena A, const double *__restrict__ V) {
+    __shared__ double sX[XR][XCP];
+    __shared__ double sT[XR][TJ];
+    const int4 t = A.tiles[blockIdx.x];
+    const int o = t.x, i0 = t.y, j0 = t.z;
     const int n0 = A.n0[o], n1 = A.n1[o];
-    const int64_t N = (int64_t)n0 * n1;
-    const int64_t pl = (int64_t)t.y + threadIdx.x;
-    if (pl >= N) return;
-    const int i = (int)(pl / n1), j = (int)(pl - (int64_t)i * n1);
-    const int64_t P = A.P, p0 = A.p_off[o], p = p0 + pl;
     const int fl = A.oflags[o];
-    const bool slow = fl & OPT_S_LOW_DIR, shigh = fl & OPT_S_HIGH_DIR, mixed = fl & OPT_MIXED;
-    const int64_t js = A.v_off[o] + j;
-    const double gl = A.dirS[js], gh = A.dirS[A.SV + js];
-    const double *Vo = V + p0;
+    const int64_t P = A.P, p0 = A.p_off[o];
+    const double *X = (MODE == ST_HV3 ? A.Y2 : V) + p0;
+    const int tid = threadIdx.x;
+    for (int e = tid; e < XR * XC; e += EXPL_THREADS) {
+        const int rr = e / XC, cc = e - rr * XC;
+        const int ii = i0 - 1 + rr, jj = j0 - 2 + cc;
+        sX[rr][cc] = (ii >= 0 && ii < n0 && jj >= 0 && jj < n1) ? X[(int64_t)ii * n1 + jj] : 0.0;
+    }
+    __syncthreads();
+    const bool mixed = fl & OPT_MIXED;
+    const int64_t vo = A.v_off[o], so = A.s_off[o];
+    if (mixed) {
+        // mixed stencil row sums t(r, j) = sum_b w1[b](j) X(r, j + b)
+        for (int e = tid; e < XR * TJ; e += EXPL_THREADS) {
+            const int rr = e / TJ, cc = e - rr * TJ;
+            const int jj = j0 + cc;
+            double s = 0.0;
+            if (jj > 0 && jj < n1 - 1)
+                s = A.w1[vo + jj] * sX[rr][cc + 1] + A.w1[A.SV + vo + jj] * sX[rr][cc + 2] +
+                    A.w1[2 * A.SV + vo + jj] * sX[rr][cc + 3];
+            sT[rr][cc] = s;
+        }
+        __syncthreads();
+    }
+    const int ty = tid / TJ, tx = tid - ty * TJ;
+    const int i = i0 + ty, j = j0 + tx;
+    if (i >= n0 || j >= n1) return;
+    const int64_t pl = (int64_t)i * n1 + j, p = p0 + pl;
+    const int64_t js = vo + j;
+    const bool slow = fl & OPT_S_LOW_DIR, shigh = fl & OPT_S_HIGH_DIR;
 
-    // F0 x: spot operator along the column through (i, j), forced Dirichlet rows
-    auto spot_apply = [&](auto X) -> double {
-        if (i == 0 && slow) return gl;
-        if (i == n0 - 1 && shigh) return gh;
-        auto xs = [&](int ii) -> double {
-            if (ii == 0 && slow) return gl;
-            if (ii == n0 - 1 && shigh) return gh;
-            return X((int64_t)ii * n1 + j);
-        };
-        double acc = 0.0;
-        if (i + 1 < n0) acc += A.F0[2 * P + p] * xs(i + 1);
-        acc += A.F0[P + p] * xs(i);
-        if (i > 0) acc += A.F0[p] * xs(i - 1);
-        return acc;
-    };
-    // F1 x: variance operator along the row through (i, j)
-    auto var_apply = [&](auto X) -> double {
-        const int64_t b = (int64_t)i * n1;
-        double acc = 0.0;
-        if (j + 1 < n1) acc += A.F1[2 * P + p] * X(b + j + 1);
-        acc += A.F1[P + p] * X(b + j);
-        if (j > 0) acc += A.F1[p] * X(b + j - 1);
-        if (j == n1 - 1) acc += A.F1x[A.s_off[o] + i] * X(b + n1 - 3);
-        return acc;
-    };
-    // M x: c * sum_a w0[a](i) sum_b w1[b](j) x(i+a, j+b), zero on the edges
-    auto mixed_apply = [&](auto X, const double *c) -> double {
-        if (!mixed || i == 0 || i == n0 - 1 || j == 0 || j == n1 - 1) return 0.0;
-        const int64_t si = A.s_off[o] + i, vj = A.v_off[o] + j;
-        const double b0 = A.w1[vj], b1 = A.w1[A.SV + vj], b2 = A.w1[2 * A.SV + vj];
-        const int64_t q = (int64_t)i * n1 + j;
-        const double tm = b0 * X(q - n1 - 1) + b1 * X(q - n1) + b2 * X(q - n1 + 1);
-        const double tc = b0 * X(q - 1) + b1 * X(q) + b2 * X(q + 1);
-        const double tp = b0 * X(q + n1 - 1) + b1 * X(q + n1) + b2 * X(q + n1 + 1);
-        return c[p] * (A.w0[si] * tm + A.w0[A.SS + si] * tc + A.w0[2 * A.SS + si] * tp);
-    };
-    auto Xv = [&](int64_t q) -> double { return __ldg(Vo + q); };
-
+    double m = 0.0;
+    if (mixed && i > 0 && i < n0 - 1 && j > 0 && j < n1 - 1) {
+        const double *c = (MODE == ST_IMPLICIT) ? A.cMi : A.cM;
+        m = c[p] * (A.w0[so + i] * sT[ty][tx] + A.w0[A.SS + so + i] * sT[ty + 1][tx] +
+                    A.w0[2 * A.SS + so + i] * sT[ty + 2][tx]);
+    }
+    const double xc = sX[ty + 1][tx + 2];
     if (MODE == ST_IMPLICIT) {
-        A.W[p] = Vo[pl] + mixed_apply(Xv, A.cMi);
+        A.W[p] = xc + m;
         return;
     }
+    // spot operator with the Dirichlet rows forced (BandedOperator.pyx:339-344)
+    const double gl = A.dirS[js], gh = A.dirS[A.SV + js];
+    double a0;
+    if (i == 0 && slow) a0 = gl;
+    else if (i == n0 - 1 && shigh) a0 = gh;
+    else {
+        const double xm = (i == 1 && slow) ? gl : sX[ty][tx + 2];
+        const double xp = (i == n0 - 2 && shigh) ? gh : sX[ty + 2][tx + 2];
+        a0 = A.F0[p] * xm + A.F0[P + p] * xc + A.F0[2 * P + p] * xp;
+    }
+    // variance operator (1-D on S > 0, diagonal on S = 0)
+    double a1;
+    if (i == 0 && (fl & OPT_ROW0_ZERO)) {
+        a1 = A.F1z[o] * xc;
+    } else {
+        a1 = A.F1v[js] * sX[ty + 1][tx + 1] + A.F1v[A.SV + js] * xc +
+             A.F1v[2 * A.SV + js] * sX[ty + 1][tx + 3];
+        if (j == n1 - 1) a1 += A.F1x[o] * sX[ty + 1][tx];
+    }
+    const double R = (i == n0 - 1) ? A.R0top[js] : 0.0;
     const double theta = A.theta[o];
     if (MODE == ST_DOUGLAS || MODE == ST_HV0) {
-        const double a0 = spot_apply(Xv), a1 = var_apply(Xv), m = mixed_apply(Xv, A.cM);
-        const double y = Vo[pl] + (a0 + A.R0[p]) + (a1 + A.R1[p]) + m;
-        if (MODE == ST_HV0) A.Y0[p] = y;
-        A.W[p] = y - theta * a0;
+        // Y0 = V + F(V) + R; right-hand side of the spot solve Y0 - theta F0 V
+        const double fv = a0 + a1 + m;
+        if (MODE == ST_HV0) A.FV[p] = fv;
+        A.W[p] = (xc + R) + fv - theta * a0;
         A.T[p] = theta * a1;
         return;
     }
-    // ST_HV3: W = Y0 - F(V - Y2)/2 (no residual) - theta F0 Y2; T = theta F1 Y2
-    const double *Y2o = A.Y2 + p0;
-    auto Xd = [&](int64_t q) -> double { return __ldg(Vo + q) - __ldg(Y2o + q); };
-    auto Xy = [&](int64_t q) -> double { return __ldg(Y2o + q); };
-    const double d = spot_apply(Xd) + var_apply(Xd) + mixed_apply(Xd, A.cM);
-    const double ay0 = spot_apply(Xy), ay1 = var_apply(Xy);
-    A.W[p] = A.Y0[p] - 0.5 * d - theta * ay0;
-    A.T[p] = theta * ay1;
+    // ST_HV3: Y0 - F(V - Y2)/2 = V + R + (F V + F Y2)/2, minus theta F0 Y2
+    const double fy = a0 + a1 + m;
+    A.W[p] = (V[p] + R) + 0.5 * (A.FV[p] + fy) - theta * a0;
+    A.T[p] = theta * a1;
 }
 
 // Spot-line solve, one thread per grid column. src -> dst (may alias).
-// RESID: subtract the implicit plan's residual. SUBT: write x - T (the next
+// IMPLICIT: implicit-plan factors and residual. SUBT: write x - T (the next
 // stage's right-hand side) instead of x.
 template <bool IMPLICIT, bool SUBT>
 __global__ void __launch_bounds__(SOLVE_THREADS) spot_solve_kernel(Arena A, const double *src,
@@ -426,7 +467,7 @@ __global__ void __launch_bounds__(SOLVE_THREADS) spot_solve_kernel(Arena A, cons
         if (i == 0 && slow) rk = gl;
         else if (i == n0 - 1 && shigh) rk = gh;
         else rk = src[p];
-        if (IMPLICIT) rk = rk - A.RSi[p];
+        if (IMPLICIT && i == n0 - 1) rk = rk - A.RSi[js];
         dp = (i == 0) ? rk * L[P + p] : (rk - L[p] * dp) * L[P + p];
         dst[p] = dp;
     }
@@ -442,35 +483,74 @@ __global__ void __launch_bounds__(SOLVE_THREADS) spot_solve_kernel(Arena A, cons
     }
 }
 
-// Variance-line solve, one thread per grid row; the bottom row of the
-// right-hand side is folded with the line's fold factor.
+// Variance-line solve: one warp per task of up to 32 consecutive grid rows of
+// one option (lane = row). Chunks of 32 columns are loaded row by row
+// (coalesced) into a padded shared tile, each lane runs its row's recurrence
+// over the chunk, and the chunk is stored back row by row. The bottom row of
+// the right-hand side is folded with the option's fold factor.
 template <bool IMPLICIT>
-__global__ void __launch_bounds__(SOLVE_THREADS) var_solve_kernel(Arena A, const double *src,
-                                                                  double *dst) {
-    const int64_t line = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (line >= A.SS) return;
-    const int o = A.lineV[line];
+__global__ void __launch_bounds__(VS_WARPS * 32) var_solve_kernel(Arena A, int n_tasks,
+                                                                  const double *src, double *dst) {
+    __shared__ double tile[VS_WARPS][32][VS_PITCH];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int task = blockIdx.x * VS_WARPS + warp;
+    if (task >= n_tasks) return;
+    const int4 tk = A.vtasks[task];
+    const int o = tk.x, i0 = tk.y, rows = tk.z;
     const int n1 = A.n1[o];
-    const int64_t i = line - A.s_off[o];
-    const int64_t P = A.P, b = A.p_off[o] + i * n1;
-    const double *L = IMPLICIT ? A.LVi : A.LV;
-    const double f = IMPLICIT ? A.foldVi[line] : A.foldV[line];
+    const int64_t base = A.p_off[o] + (int64_t)i0 * n1;
+    const int64_t vo = A.v_off[o], SV = A.SV;
+    const double *L = IMPLICIT ? A.LVvi : A.LVv;
+    const double f = IMPLICIT ? A.foldVi[o] : A.foldV[o];
+    const double z = IMPLICIT ? A.LVzi[o] : A.LVz[o];
+    const bool special = (i0 + lane == 0) && (A.oflags[o] & OPT_ROW0_ZERO);
+    double(*tl)[VS_PITCH] = tile[warp];
+    const int nch = (n1 + 31) >> 5;
     double dp = 0.0, rprev = 0.0;
-    for (int j = 0; j < n1; ++j) {
-        const int64_t p = b + j;
-        double rk = src[p];
-        if (IMPLICIT) rk = rk - A.RVi[p];
-        const double raw = rk;
-        if (j == n1 - 1) rk += 1.0 * rprev * f;
-        dp = (j == 0) ? rk * L[P + p] : (rk - L[p] * dp) * L[P + p];
-        dst[p] = dp;
-        rprev = raw;
+    for (int ch = 0; ch < nch; ++ch) {
+        const int c0 = ch << 5, w = min(32, n1 - c0);
+        for (int rr = 0; rr < rows; ++rr)
+            tl[rr][lane] = lane < w ? src[base + (int64_t)rr * n1 + c0 + lane] : 0.0;
+        __syncwarp();
+        if (lane < rows) {
+            for (int c = 0; c < w; ++c) {
+                const int col = c0 + c;
+                double rk = tl[lane][c];
+                const double raw = rk;
+                if (special) {
+                    dp = rk * z;
+                } else {
+                    if (col == n1 - 1) rk += 1.0 * rprev * f;
+                    const double inv = L[SV + vo + col];
+                    dp = (col == 0) ? rk * inv : (rk - L[vo + col] * dp) * inv;
+                }
+                tl[lane][c] = dp;
+                rprev = raw;
+            }
+        }
+        __syncwarp();
+        for (int rr = 0; rr < rows; ++rr)
+            if (lane < w) dst[base + (int64_t)rr * n1 + c0 + lane] = tl[rr][lane];
+        __syncwarp();
     }
-    double x = dp;
-    for (int j = n1 - 2; j >= 0; --j) {
-        const int64_t p = b + j;
-        x = dst[p] - L[2 * P + p] * x;
-        dst[p] = x;
+    double x = 0.0;
+    for (int ch = nch - 1; ch >= 0; --ch) {
+        const int c0 = ch << 5, w = min(32, n1 - c0);
+        for (int rr = 0; rr < rows; ++rr)
+            tl[rr][lane] = lane < w ? dst[base + (int64_t)rr * n1 + c0 + lane] : 0.0;
+        __syncwarp();
+        if (lane < rows) {
+            for (int c = w - 1; c >= 0; --c) {
+                const int col = c0 + c;
+                const double d = tl[lane][c];
+                x = (col == n1 - 1 || special) ? d : d - L[2 * SV + vo + col] * x;
+                tl[lane][c] = x;
+            }
+        }
+        __syncwarp();
+        for (int rr = 0; rr < rows; ++rr)
+            if (lane < w) dst[base + (int64_t)rr * n1 + c0 + lane] = tl[rr][lane];
+        __syncwarp();
     }
 }
 
@@ -503,13 +583,14 @@ static inline int64_t align256(int64_t x) { return (x + 255) & ~(int64_t)255; }
 
 struct Layout {
     int n_opt = 0;
-    int64_t P = 0, SS = 0, SV = 0, n_tiles = 0;
-    bool smoothing = false;
-    // byte offsets into the workspace
-    int64_t o_n0, o_n1, o_flags, o_p, o_s, o_v, o_lineS, o_lineV, o_tiles, o_theta;
-    int64_t o_F0, o_R0, o_F1, o_R1, o_F1x, o_cM, o_w0, o_w1, o_LS, o_LV, o_foldV, o_dirS;
-    int64_t o_cMi, o_RSi, o_RVi, o_LSi, o_LVi, o_foldVi;
-    int64_t o_Y0, o_W, o_T, o_Y2;
+    int64_t P = 0, SS = 0, SV = 0, n_tiles = 0, n_vtasks = 0;
+    bool smoothing = false, hv = false;
+    // byte offsets into the workspace (-1: absent)
+    int64_t o_n0, o_n1, o_flags, o_p, o_s, o_v, o_lineS, o_tiles, o_vtasks, o_theta;
+    int64_t o_F0, o_cM, o_w0, o_w1, o_LS, o_R0top, o_F1v, o_F1x, o_F1z, o_LVv, o_foldV, o_LVz,
+        o_dirS;
+    int64_t o_cMi, o_RSi, o_LSi, o_LVvi, o_foldVi, o_LVzi;
+    int64_t o_FV, o_W, o_T, o_Y2;
     int64_t bytes = 0;
     std::vector<int64_t> p_off, s_off, v_off;
 };
@@ -525,6 +606,7 @@ static int make_layout(const fdadi_heston_batch_t *b, Layout &L) {
                   "implicit_dt_factor must be positive");
     L.n_opt = b->n_options;
     L.smoothing = b->implicit_steps > 0;
+    L.hv = b->scheme == FDADI_SCHEME_HV;
     L.p_off.resize(L.n_opt + 1);
     L.s_off.resize(L.n_opt + 1);
     L.v_off.resize(L.n_opt + 1);
@@ -537,33 +619,35 @@ static int make_layout(const fdadi_heston_batch_t *b, Layout &L) {
         L.p_off[k + 1] = L.p_off[k] + N;
         L.s_off[k + 1] = L.s_off[k] + b->n0[k];
         L.v_off[k + 1] = L.v_off[k] + b->n1[k];
-        L.n_tiles += (N + EXPL_TILE - 1) / EXPL_TILE;
+        L.n_tiles += (int64_t)((b->n0[k] + TI - 1) / TI) * ((b->n1[k] + TJ - 1) / TJ);
+        L.n_vtasks += (b->n0[k] + 31) / 32;
     }
     L.P = L.p_off[L.n_opt];
     L.SS = L.s_off[L.n_opt];
     L.SV = L.v_off[L.n_opt];
-    FDADI_REQUIRE(L.n_tiles < (int64_t)1 << 31, "batch too large");
+    FDADI_REQUIRE(L.n_tiles < ((int64_t)1 << 31) && L.n_vtasks < ((int64_t)1 << 31),
+                  "batch too large");
     int64_t off = 0;
     auto take = [&](int64_t bytes) { int64_t o = off; off = align256(off + bytes); return o; };
-    const int64_t D = sizeof(double);
-    L.o_n0 = take(4 * L.n_opt); L.o_n1 = take(4 * L.n_opt); L.o_flags = take(4 * L.n_opt);
-    L.o_p = take(8 * L.n_opt); L.o_s = take(8 * L.n_opt); L.o_v = take(8 * L.n_opt);
-    L.o_lineS = take(4 * L.SV); L.o_lineV = take(4 * L.SS); L.o_tiles = take(8 * L.n_tiles);
-    L.o_theta = take(D * L.n_opt);
-    L.o_F0 = take(3 * D * L.P); L.o_R0 = take(D * L.P); L.o_F1 = take(3 * D * L.P);
-    L.o_R1 = take(D * L.P); L.o_F1x = take(D * L.SS); L.o_cM = take(D * L.P);
+    const int64_t D = sizeof(double), N = L.n_opt;
+    L.o_n0 = take(4 * N); L.o_n1 = take(4 * N); L.o_flags = take(4 * N);
+    L.o_p = take(8 * N); L.o_s = take(8 * N); L.o_v = take(8 * N);
+    L.o_lineS = take(4 * L.SV); L.o_tiles = take(16 * L.n_tiles);
+    L.o_vtasks = take(16 * L.n_vtasks); L.o_theta = take(D * N);
+    L.o_F0 = take(3 * D * L.P); L.o_cM = take(D * L.P);
     L.o_w0 = take(3 * D * L.SS); L.o_w1 = take(3 * D * L.SV);
-    L.o_LS = take(3 * D * L.P); L.o_LV = take(3 * D * L.P); L.o_foldV = take(D * L.SS);
-    L.o_dirS = take(2 * D * L.SV);
+    L.o_LS = take(3 * D * L.P); L.o_R0top = take(D * L.SV); L.o_F1v = take(3 * D * L.SV);
+    L.o_F1x = take(D * N); L.o_F1z = take(D * N); L.o_LVv = take(3 * D * L.SV);
+    L.o_foldV = take(D * N); L.o_LVz = take(D * N); L.o_dirS = take(2 * D * L.SV);
     if (L.smoothing) {
-        L.o_cMi = take(D * L.P); L.o_RSi = take(D * L.P); L.o_RVi = take(D * L.P);
-        L.o_LSi = take(3 * D * L.P); L.o_LVi = take(3 * D * L.P); L.o_foldVi = take(D * L.SS);
+        L.o_cMi = take(D * L.P); L.o_RSi = take(D * L.SV); L.o_LSi = take(3 * D * L.P);
+        L.o_LVvi = take(3 * D * L.SV); L.o_foldVi = take(D * N); L.o_LVzi = take(D * N);
     } else {
-        L.o_cMi = L.o_RSi = L.o_RVi = L.o_LSi = L.o_LVi = L.o_foldVi = -1;
+        L.o_cMi = L.o_RSi = L.o_LSi = L.o_LVvi = L.o_foldVi = L.o_LVzi = -1;
     }
     L.o_W = take(D * L.P); L.o_T = take(D * L.P);
-    if (b->scheme == FDADI_SCHEME_HV) { L.o_Y0 = take(D * L.P); L.o_Y2 = take(D * L.P); }
-    else L.o_Y0 = L.o_Y2 = -1;
+    if (L.hv) { L.o_FV = take(D * L.P); L.o_Y2 = take(D * L.P); }
+    else L.o_FV = L.o_Y2 = -1;
     L.bytes = off;
     return FDADI_OK;
 }
@@ -576,74 +660,110 @@ static Arena arena_view(const Layout &L, char *ws) {
     A.oflags = (const int *)(ws + L.o_flags);
     A.p_off = (const int64_t *)(ws + L.o_p); A.s_off = (const int64_t *)(ws + L.o_s);
     A.v_off = (const int64_t *)(ws + L.o_v);
-    A.lineS = (const int *)(ws + L.o_lineS); A.lineV = (const int *)(ws + L.o_lineV);
-    A.tiles = (const int2 *)(ws + L.o_tiles);
+    A.lineS = (const int *)(ws + L.o_lineS);
+    A.tiles = (const int4 *)(ws + L.o_tiles);
+    A.vtasks = (const int4 *)(ws + L.o_vtasks);
     A.theta = ptr(L.o_theta);
-    A.F0 = ptr(L.o_F0); A.R0 = ptr(L.o_R0); A.F1 = ptr(L.o_F1); A.R1 = ptr(L.o_R1);
-    A.F1x = ptr(L.o_F1x); A.cM = ptr(L.o_cM); A.w0 = ptr(L.o_w0); A.w1 = ptr(L.o_w1);
-    A.LS = ptr(L.o_LS); A.LV = ptr(L.o_LV); A.foldV = ptr(L.o_foldV); A.dirS = ptr(L.o_dirS);
-    A.cMi = ptr(L.o_cMi); A.RSi = ptr(L.o_RSi); A.RVi = ptr(L.o_RVi); A.LSi = ptr(L.o_LSi);
-    A.LVi = ptr(L.o_LVi); A.foldVi = ptr(L.o_foldVi);
-    A.Y0 = ptr(L.o_Y0); A.W = ptr(L.o_W); A.T = ptr(L.o_T); A.Y2 = ptr(L.o_Y2);
+    A.F0 = ptr(L.o_F0); A.cM = ptr(L.o_cM); A.w0 = ptr(L.o_w0); A.w1 = ptr(L.o_w1);
+    A.LS = ptr(L.o_LS); A.R0top = ptr(L.o_R0top); A.F1v = ptr(L.o_F1v); A.F1x = ptr(L.o_F1x);
+    A.F1z = ptr(L.o_F1z); A.LVv = ptr(L.o_LVv); A.foldV = ptr(L.o_foldV); A.LVz = ptr(L.o_LVz);
+    A.dirS = ptr(L.o_dirS);
+    A.cMi = ptr(L.o_cMi); A.RSi = ptr(L.o_RSi); A.LSi = ptr(L.o_LSi); A.LVvi = ptr(L.o_LVvi);
+    A.foldVi = ptr(L.o_foldVi); A.LVzi = ptr(L.o_LVzi);
+    A.FV = ptr(L.o_FV); A.W = ptr(L.o_W); A.T = ptr(L.o_T); A.Y2 = ptr(L.o_Y2);
     return A;
+}
+
+struct Grids {
+    unsigned tiles, spot, var;
+    int n_vtasks;
+};
+
+static Grids grids(const Layout &L) {
+    return Grids{(unsigned)L.n_tiles, (unsigned)((L.SV + SOLVE_THREADS - 1) / SOLVE_THREADS),
+                 (unsigned)((L.n_vtasks + VS_WARPS - 1) / VS_WARPS), (int)L.n_vtasks};
+}
+
+static void launch_stage(int stage, const Grids &g, const Arena &A, double *V, cudaStream_t st) {
+    switch (stage) {
+    case FDADI_STAGE_EXPLICIT_DOUGLAS:
+        explicit_kernel<ST_DOUGLAS><<<g.tiles, EXPL_THREADS, 0, st>>>(A, V); break;
+    case FDADI_STAGE_EXPLICIT_HV0:
+        explicit_kernel<ST_HV0><<<g.tiles, EXPL_THREADS, 0, st>>>(A, V); break;
+    case FDADI_STAGE_EXPLICIT_HV3:
+        explicit_kernel<ST_HV3><<<g.tiles, EXPL_THREADS, 0, st>>>(A, V); break;
+    case FDADI_STAGE_EXPLICIT_IMPLICIT:
+        explicit_kernel<ST_IMPLICIT><<<g.tiles, EXPL_THREADS, 0, st>>>(A, V); break;
+    case FDADI_STAGE_SPOT_SOLVE:
+        spot_solve_kernel<false, true><<<g.spot, SOLVE_THREADS, 0, st>>>(A, A.W, A.W); break;
+    case FDADI_STAGE_VAR_SOLVE_TO_Y2:
+        var_solve_kernel<false><<<g.var, VS_WARPS * 32, 0, st>>>(A, g.n_vtasks, A.W, A.Y2); break;
+    case FDADI_STAGE_VAR_SOLVE_TO_V:
+        var_solve_kernel<false><<<g.var, VS_WARPS * 32, 0, st>>>(A, g.n_vtasks, A.W, V); break;
+    case FDADI_STAGE_VAR_SOLVE_IMPLICIT:
+        var_solve_kernel<true><<<g.var, VS_WARPS * 32, 0, st>>>(A, g.n_vtasks, A.W, A.W); break;
+    case FDADI_STAGE_SPOT_SOLVE_IMPLICIT:
+        spot_solve_kernel<true, false><<<g.spot, SOLVE_THREADS, 0, st>>>(A, A.W, V); break;
+    default: break;
+    }
 }
 
 // Launch sequence of the time loop (shared by the direct path and the graph
 // capture).
 static int launch_steps(const fdadi_heston_batch_t *b, const Layout &L, const Arena &A, double *V,
-                        cudaStream_t st, int64_t *count) {
-    const unsigned tiles = (unsigned)L.n_tiles;
-    const unsigned gS = (unsigned)((L.SV + SOLVE_THREADS - 1) / SOLVE_THREADS);
-    const unsigned gV = (unsigned)((L.SS + SOLVE_THREADS - 1) / SOLVE_THREADS);
-    int64_t n = 0;
+                        cudaStream_t st) {
+    const Grids g = grids(L);
     for (int s = 0; s < b->implicit_steps; ++s) {
-        explicit_kernel<ST_IMPLICIT><<<tiles, EXPL_TILE, 0, st>>>(A, V);
-        var_solve_kernel<true><<<gV, SOLVE_THREADS, 0, st>>>(A, A.W, A.W);
-        spot_solve_kernel<true, false><<<gS, SOLVE_THREADS, 0, st>>>(A, A.W, V);
-        n += 3;
+        launch_stage(FDADI_STAGE_EXPLICIT_IMPLICIT, g, A, V, st);
+        launch_stage(FDADI_STAGE_VAR_SOLVE_IMPLICIT, g, A, V, st);
+        launch_stage(FDADI_STAGE_SPOT_SOLVE_IMPLICIT, g, A, V, st);
     }
     for (int s = 0; s < b->n_steps; ++s) {
         if (b->scheme == FDADI_SCHEME_DOUGLAS) {
-            explicit_kernel<ST_DOUGLAS><<<tiles, EXPL_TILE, 0, st>>>(A, V);
-            spot_solve_kernel<false, true><<<gS, SOLVE_THREADS, 0, st>>>(A, A.W, A.W);
-            var_solve_kernel<false><<<gV, SOLVE_THREADS, 0, st>>>(A, A.W, V);
-            n += 3;
+            launch_stage(FDADI_STAGE_EXPLICIT_DOUGLAS, g, A, V, st);
+            launch_stage(FDADI_STAGE_SPOT_SOLVE, g, A, V, st);
+            launch_stage(FDADI_STAGE_VAR_SOLVE_TO_V, g, A, V, st);
         } else {
-            explicit_kernel<ST_HV0><<<tiles, EXPL_TILE, 0, st>>>(A, V);
-            spot_solve_kernel<false, true><<<gS, SOLVE_THREADS, 0, st>>>(A, A.W, A.W);
-            var_solve_kernel<false><<<gV, SOLVE_THREADS, 0, st>>>(A, A.W, A.Y2);
-            explicit_kernel<ST_HV3><<<tiles, EXPL_TILE, 0, st>>>(A, V);
-            spot_solve_kernel<false, true><<<gS, SOLVE_THREADS, 0, st>>>(A, A.W, A.W);
-            var_solve_kernel<false><<<gV, SOLVE_THREADS, 0, st>>>(A, A.W, V);
-            n += 6;
+            launch_stage(FDADI_STAGE_EXPLICIT_HV0, g, A, V, st);
+            launch_stage(FDADI_STAGE_SPOT_SOLVE, g, A, V, st);
+            launch_stage(FDADI_STAGE_VAR_SOLVE_TO_Y2, g, A, V, st);
+            launch_stage(FDADI_STAGE_EXPLICIT_HV3, g, A, V, st);
+            launch_stage(FDADI_STAGE_SPOT_SOLVE, g, A, V, st);
+            launch_stage(FDADI_STAGE_VAR_SOLVE_TO_V, g, A, V, st);
         }
     }
-    if (count) *count = n;
     FDADI_CHECK_LAUNCH();
     return FDADI_OK;
 }
 
 // Instantiated graphs of the time loop, keyed by everything the launches
-// capture (workspace, state pointer, schedule).
+// capture (workspace, state pointer, schedule, launch geometry).
 struct GraphKey {
     const void *ws; const void *V; int n_opt, scheme, n_steps, smoothing;
-    double factor, theta;
-    int64_t P, SS, SV, n_tiles;
+    int64_t P, SS, SV, n_tiles, n_vtasks;
     bool operator==(const GraphKey &o) const {
         return ws == o.ws && V == o.V && n_opt == o.n_opt && scheme == o.scheme &&
                n_steps == o.n_steps && smoothing == o.smoothing && P == o.P && SS == o.SS &&
-               factor == o.factor && theta == o.theta &&
-               SV == o.SV && n_tiles == o.n_tiles;
+               SV == o.SV && n_tiles == o.n_tiles && n_vtasks == o.n_vtasks;
     }
 };
 struct GraphKeyHash {
     size_t operator()(const GraphKey &k) const {
         return std::hash<const void *>()(k.ws) ^ (std::hash<const void *>()(k.V) << 1) ^
-               ((size_t)k.n_steps << 7) ^ ((size_t)k.n_opt << 19);
+               ((size_t)k.n_steps << 7) ^ ((size_t)k.n_opt << 19) ^ ((size_t)k.P << 3);
     }
 };
 static std::mutex g_graph_mu;
 static std::unordered_map<GraphKey, cudaGraphExec_t, GraphKeyHash> g_graphs;
+
+static int check_ws(const Layout &L, void *ws, int64_t bytes) {
+    FDADI_REQUIRE(ws != nullptr, "null workspace");
+    if (bytes < L.bytes) {
+        set_error("workspace too small: %lld < %lld bytes", (long long)bytes, (long long)L.bytes);
+        return FDADI_E_WORKSPACE;
+    }
+    return FDADI_OK;
+}
 
 }  // namespace fdadi
 
@@ -668,36 +788,25 @@ int fdadi_heston_prepare(const fdadi_heston_batch_t *b, void *workspace, int64_t
     Layout L;
     int rc = make_layout(b, L);
     if (rc) return rc;
-    FDADI_REQUIRE(workspace != nullptr, "null workspace");
-    if (ws_bytes < L.bytes) {
-        set_error("workspace too small: %lld < %lld bytes", (long long)ws_bytes, (long long)L.bytes);
-        return FDADI_E_WORKSPACE;
-    }
+    rc = check_ws(L, workspace, ws_bytes);
+    if (rc) return rc;
     FDADI_REQUIRE(b->spots && b->vars && b->params && b->dt, "null mesh/params/dt pointer");
     cudaStream_t st = as_stream(stream);
     char *ws = (char *)workspace;
-    // host tables
-    std::vector<int> n0(L.n_opt), n1(L.n_opt), flags(L.n_opt), lineS(L.SV), lineV(L.SS);
-    std::vector<int2> tiles;
+    // host tables (flags are completed on the device)
+    std::vector<int> n0(L.n_opt), n1(L.n_opt), flags(L.n_opt, 0), lineS(L.SV);
+    std::vector<int4> tiles, vtasks;
     tiles.reserve(L.n_tiles);
+    vtasks.reserve(L.n_vtasks);
     std::vector<double> theta(L.n_opt, b->theta);
-    std::vector<int> barrier(L.n_opt, 0);
-    if (b->barrier)
-        FDADI_CUDA(cudaMemcpyAsync(barrier.data(), b->barrier, 4 * L.n_opt, cudaMemcpyDeviceToHost, st));
-    // rho per option decides whether the mixed operator runs
-    std::vector<double> params(5 * (size_t)L.n_opt);
-    FDADI_CUDA(cudaMemcpyAsync(params.data(), b->params, 8 * params.size(), cudaMemcpyDeviceToHost, st));
-    FDADI_CUDA(cudaStreamSynchronize(st));
     for (int k = 0; k < L.n_opt; ++k) {
         n0[k] = b->n0[k];
         n1[k] = b->n1[k];
-        const double rho = params[5 * (size_t)k + 4];
-        const bool mixed = !((b->flags & FDADI_HESTON_DROP_ZERO_MIXED) && rho == 0.0);
-        flags[k] = OPT_S_LOW_DIR | (barrier[k] ? OPT_S_HIGH_DIR : 0) | (mixed ? OPT_MIXED : 0);
         for (int64_t j = L.v_off[k]; j < L.v_off[k + 1]; ++j) lineS[j] = k;
-        for (int64_t i = L.s_off[k]; i < L.s_off[k + 1]; ++i) lineV[i] = k;
-        const int64_t N = L.p_off[k + 1] - L.p_off[k];
-        for (int64_t t = 0; t < N; t += EXPL_TILE) tiles.push_back(make_int2(k, (int)t));
+        for (int i0 = 0; i0 < n0[k]; i0 += TI)
+            for (int j0 = 0; j0 < n1[k]; j0 += TJ) tiles.push_back(make_int4(k, i0, j0, 0));
+        for (int i0 = 0; i0 < n0[k]; i0 += 32)
+            vtasks.push_back(make_int4(k, i0, std::min(32, n0[k] - i0), 0));
     }
     FDADI_CUDA(cudaMemcpyAsync(ws + L.o_n0, n0.data(), 4 * L.n_opt, cudaMemcpyHostToDevice, st));
     FDADI_CUDA(cudaMemcpyAsync(ws + L.o_n1, n1.data(), 4 * L.n_opt, cudaMemcpyHostToDevice, st));
@@ -706,17 +815,17 @@ int fdadi_heston_prepare(const fdadi_heston_batch_t *b, void *workspace, int64_t
     FDADI_CUDA(cudaMemcpyAsync(ws + L.o_s, L.s_off.data(), 8 * L.n_opt, cudaMemcpyHostToDevice, st));
     FDADI_CUDA(cudaMemcpyAsync(ws + L.o_v, L.v_off.data(), 8 * L.n_opt, cudaMemcpyHostToDevice, st));
     FDADI_CUDA(cudaMemcpyAsync(ws + L.o_lineS, lineS.data(), 4 * L.SV, cudaMemcpyHostToDevice, st));
-    FDADI_CUDA(cudaMemcpyAsync(ws + L.o_lineV, lineV.data(), 4 * L.SS, cudaMemcpyHostToDevice, st));
-    FDADI_CUDA(cudaMemcpyAsync(ws + L.o_tiles, tiles.data(), 8 * tiles.size(), cudaMemcpyHostToDevice, st));
+    FDADI_CUDA(cudaMemcpyAsync(ws + L.o_tiles, tiles.data(), 16 * tiles.size(), cudaMemcpyHostToDevice, st));
+    FDADI_CUDA(cudaMemcpyAsync(ws + L.o_vtasks, vtasks.data(), 16 * vtasks.size(), cudaMemcpyHostToDevice, st));
     FDADI_CUDA(cudaMemcpyAsync(ws + L.o_theta, theta.data(), 8 * L.n_opt, cudaMemcpyHostToDevice, st));
     Arena A = arena_view(L, ws);
     BuildArgs a{b->spots, b->vars, b->params, b->dt, b->barrier, b->theta, b->implicit_dt_factor,
-                L.smoothing ? 1 : 0};
-    build_points_kernel<<<(unsigned)L.n_tiles, EXPL_TILE, 0, st>>>(A, a);
+                L.smoothing ? 1 : 0, (b->flags & FDADI_HESTON_DROP_ZERO_MIXED) ? 1 : 0};
+    build_options_kernel<<<(unsigned)((L.n_opt + 127) / 128), 128, 0, st>>>(A, a);
+    FDADI_CHECK_LAUNCH();
+    build_points_kernel<<<(unsigned)L.n_tiles, EXPL_THREADS, 0, st>>>(A, a);
     FDADI_CHECK_LAUNCH();
     build_spot_lines_kernel<<<(unsigned)((L.SV + 127) / 128), 128, 0, st>>>(A, a);
-    FDADI_CHECK_LAUNCH();
-    build_var_lines_kernel<<<(unsigned)((L.SS + 127) / 128), 128, 0, st>>>(A, a);
     FDADI_CHECK_LAUNCH();
     // the host tables must outlive the copies
     FDADI_CUDA(cudaStreamSynchronize(st));
@@ -728,17 +837,15 @@ int fdadi_heston_run(const fdadi_heston_batch_t *b, void *workspace, int64_t ws_
     Layout L;
     int rc = make_layout(b, L);
     if (rc) return rc;
-    FDADI_REQUIRE(workspace && V, "null workspace or state");
-    if (ws_bytes < L.bytes) {
-        set_error("workspace too small: %lld < %lld bytes", (long long)ws_bytes, (long long)L.bytes);
-        return FDADI_E_WORKSPACE;
-    }
+    rc = check_ws(L, workspace, ws_bytes);
+    if (rc) return rc;
+    FDADI_REQUIRE(V != nullptr, "null state");
     cudaStream_t st = as_stream(stream);
     Arena A = arena_view(L, (char *)workspace);
-    if (!(b->flags & FDADI_HESTON_GRAPH)) return launch_steps(b, L, A, V, st, nullptr);
+    if (!(b->flags & FDADI_HESTON_GRAPH)) return launch_steps(b, L, A, V, st);
     FDADI_REQUIRE(st != nullptr, "graph mode needs a non-default stream");
     GraphKey key{workspace, V, b->n_options, b->scheme, b->n_steps, b->implicit_steps,
-                 b->implicit_dt_factor, b->theta, L.P, L.SS, L.SV, L.n_tiles};
+                 L.P, L.SS, L.SV, L.n_tiles, L.n_vtasks};
     cudaGraphExec_t exec = nullptr;
     {
         std::lock_guard<std::mutex> g(g_graph_mu);
@@ -748,7 +855,7 @@ int fdadi_heston_run(const fdadi_heston_batch_t *b, void *workspace, int64_t ws_
     if (!exec) {
         cudaGraph_t graph;
         FDADI_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        int lrc = launch_steps(b, L, A, V, st, nullptr);
+        int lrc = launch_steps(b, L, A, V, st);
         cudaError_t ec = cudaStreamEndCapture(st, &graph);
         if (lrc) return lrc;
         FDADI_CUDA(ec);
@@ -766,38 +873,20 @@ int fdadi_heston_stage(const fdadi_heston_batch_t *b, void *workspace, int64_t w
     Layout L;
     int rc = make_layout(b, L);
     if (rc) return rc;
-    FDADI_REQUIRE(workspace && V, "null workspace or state");
-    if (ws_bytes < L.bytes) {
-        set_error("workspace too small: %lld < %lld bytes", (long long)ws_bytes, (long long)L.bytes);
-        return FDADI_E_WORKSPACE;
-    }
-    const bool hv = b->scheme == FDADI_SCHEME_HV;
+    rc = check_ws(L, workspace, ws_bytes);
+    if (rc) return rc;
+    FDADI_REQUIRE(V != nullptr, "null state");
+    FDADI_REQUIRE(stage >= FDADI_STAGE_EXPLICIT_DOUGLAS && stage <= FDADI_STAGE_SPOT_SOLVE_IMPLICIT,
+                  "unknown stage %d", stage);
     FDADI_REQUIRE(!(stage == FDADI_STAGE_EXPLICIT_HV0 || stage == FDADI_STAGE_EXPLICIT_HV3 ||
-                    stage == FDADI_STAGE_VAR_SOLVE_TO_Y2) || hv,
+                    stage == FDADI_STAGE_VAR_SOLVE_TO_Y2) || L.hv,
                   "stage %d needs a Hundsdorfer-Verwer batch", stage);
-    FDADI_REQUIRE(stage < FDADI_STAGE_EXPLICIT_IMPLICIT || stage > FDADI_STAGE_SPOT_SOLVE_IMPLICIT ||
-                      stage == FDADI_STAGE_SPOT_SOLVE || stage == FDADI_STAGE_VAR_SOLVE_TO_Y2 ||
-                      stage == FDADI_STAGE_VAR_SOLVE_TO_V || L.smoothing,
+    FDADI_REQUIRE(!(stage == FDADI_STAGE_EXPLICIT_IMPLICIT ||
+                    stage == FDADI_STAGE_VAR_SOLVE_IMPLICIT ||
+                    stage == FDADI_STAGE_SPOT_SOLVE_IMPLICIT) || L.smoothing,
                   "stage %d needs a batch with implicit steps", stage);
-    cudaStream_t st = as_stream(stream);
     Arena A = arena_view(L, (char *)workspace);
-    const unsigned tiles = (unsigned)L.n_tiles;
-    const unsigned gS = (unsigned)((L.SV + SOLVE_THREADS - 1) / SOLVE_THREADS);
-    const unsigned gV = (unsigned)((L.SS + SOLVE_THREADS - 1) / SOLVE_THREADS);
-    switch (stage) {
-    case FDADI_STAGE_EXPLICIT_DOUGLAS: explicit_kernel<ST_DOUGLAS><<<tiles, EXPL_TILE, 0, st>>>(A, V); break;
-    case FDADI_STAGE_EXPLICIT_HV0: explicit_kernel<ST_HV0><<<tiles, EXPL_TILE, 0, st>>>(A, V); break;
-    case FDADI_STAGE_EXPLICIT_HV3: explicit_kernel<ST_HV3><<<tiles, EXPL_TILE, 0, st>>>(A, V); break;
-    case FDADI_STAGE_EXPLICIT_IMPLICIT: explicit_kernel<ST_IMPLICIT><<<tiles, EXPL_TILE, 0, st>>>(A, V); break;
-    case FDADI_STAGE_SPOT_SOLVE: spot_solve_kernel<false, true><<<gS, SOLVE_THREADS, 0, st>>>(A, A.W, A.W); break;
-    case FDADI_STAGE_VAR_SOLVE_TO_Y2: var_solve_kernel<false><<<gV, SOLVE_THREADS, 0, st>>>(A, A.W, A.Y2); break;
-    case FDADI_STAGE_VAR_SOLVE_TO_V: var_solve_kernel<false><<<gV, SOLVE_THREADS, 0, st>>>(A, A.W, V); break;
-    case FDADI_STAGE_VAR_SOLVE_IMPLICIT: var_solve_kernel<true><<<gV, SOLVE_THREADS, 0, st>>>(A, A.W, A.W); break;
-    case FDADI_STAGE_SPOT_SOLVE_IMPLICIT: spot_solve_kernel<true, false><<<gS, SOLVE_THREADS, 0, st>>>(A, A.W, V); break;
-    default:
-        set_error("unknown stage %d", stage);
-        return FDADI_E_ARG;
-    }
+    launch_stage(stage, grids(L), A, V, as_stream(stream));
     FDADI_CHECK_LAUNCH();
     return FDADI_OK;
 }
