@@ -484,7 +484,8 @@ def main():
                              "flops_per_point": STAGE_FLOPS[dom]},
                "stage_ms": {k: round(v[0], 4) for k, v in st.items()},
                "clocks": clk}
-        out["cpu_baseline"] = cpu_baseline(w, args.cpu_sample)
+        if args.cpu_sample > 0:
+            out["cpu_baseline"] = cpu_baseline(w, args.cpu_sample)
         if not args.no_extras:
             out["plain_vs_batched"] = plain_vs_batched(torch)
     if world > 1:

@@ -7,7 +7,7 @@
 // per-variance-index array. Each time step is a short chain of launches over
 // the whole batch:
 //
-//   explicit stage  -- 8x32-point tiles staged in shared memory with a halo:
+//   explicit stage  -- 16x32-point tiles staged in shared memory with a halo:
 //                      the spot, variance and mixed applies of F(V) fused
 //                      with the scheme's combination; the mixed stencil's
 //                      row sums are formed once per tile row and shared;
@@ -47,7 +47,7 @@ namespace fdadi {
 
 enum : int { OPT_S_LOW_DIR = 1, OPT_S_HIGH_DIR = 2, OPT_MIXED = 4, OPT_ROW0_ZERO = 8 };
 
-constexpr int TI = 8;                 // explicit tile rows
+constexpr int TI = 16;                // explicit tile rows
 constexpr int TJ = 32;                // explicit tile columns
 constexpr int EXPL_THREADS = TI * TJ;
 constexpr int XR = TI + 2;            // staged rows (one-row halo above and below)
@@ -69,8 +69,8 @@ struct Arena {
     const int4 *vtasks;        // variance-solve tasks: (option, i0, rows, -)
     // main plan (dt, theta)
     double *F0;                // [3P] spot operator rows (sub, mid, sup) * dt; Dirichlet rows identity
-    double *cM;                // [P] mixed coefficient rho sigma S v * dt
-    double *w0, *w1;           // [3 SS], [3 SV] centred first-derivative weights
+    double *w0;                // [3 SS] spot first-derivative weights * rho sigma S_i dt
+    double *w1;                // [3 SV] variance first-derivative weights * v_j
     double *LS;                // [3P] Thomas factors (a, 1/m, c') of 1 - theta dt A0
     double *R0top;             // [SV] spot residual on the S_max row * dt
     double *F1v;               // [3 SV] variance operator rows on S > 0 * dt
@@ -81,7 +81,7 @@ struct Arena {
     double *LVz;               // [n_opt] 1/diagonal of 1 - theta dt A1 on S = 0
     double *dirS;              // [2 SV] Dirichlet values of the spot lines (low, high)
     // implicit plan (dt * factor, theta = 1, residual kept)
-    double *cMi, *RSi, *LSi, *LVvi, *foldVi, *LVzi;
+    double *w0i, *RSi, *LSi, *LVvi, *foldVi, *LVzi;
     // stage buffers
     double *FV, *W, *T, *Y2;
     const double *theta;       // [n_opt]
@@ -298,20 +298,25 @@ __global__ void build_points_kernel(Arena A, BuildArgs a) {
     } else {
         A.F0[p] = MUL(s.sub, dt); A.F0[P + p] = MUL(s.mid, dt); A.F0[2 * P + p] = MUL(s.sup, dt);
     }
-    const double c = MUL(MUL(MUL(rho, sigma), S[i]), v[j]);
-    A.cM[p] = MUL(c, dt);
-    if (a.smoothing) A.cMi[p] = MUL(c, dti);
+    // mixed term rho sigma S_i v_j (D_S (x) D_v): the coefficient is
+    // separable, so it is folded into the two stencils' weights
     if (j == 0) {
         double sb = 0.0, md = 0.0, sp = 0.0;
         if (i > 0 && i < n0 - 1) centre(S, i, 1, sb, md, sp);
         const int64_t q = A.s_off[o] + i;
-        A.w0[q] = sb; A.w0[A.SS + q] = md; A.w0[2 * A.SS + q] = sp;
+        const double cs = MUL(MUL(rho, sigma), S[i]);
+        const double cm = MUL(cs, dt);
+        A.w0[q] = sb * cm; A.w0[A.SS + q] = md * cm; A.w0[2 * A.SS + q] = sp * cm;
+        if (a.smoothing) {
+            const double ci = MUL(cs, dti);
+            A.w0i[q] = sb * ci; A.w0i[A.SS + q] = md * ci; A.w0i[2 * A.SS + q] = sp * ci;
+        }
     }
     if (i == 0) {
         const int64_t q = A.v_off[o] + j;
         double sb = 0.0, md = 0.0, sp = 0.0;
         if (j > 0 && j < n1 - 1) centre(v, j, 1, sb, md, sp);
-        A.w1[q] = sb; A.w1[A.SV + q] = md; A.w1[2 * A.SV + q] = sp;
+        A.w1[q] = sb * v[j]; A.w1[A.SV + q] = md * v[j]; A.w1[2 * A.SV + q] = sp * v[j];
         A.dirS[q] = 0.0;
         A.dirS[A.SV + q] = 0.0;
         const Row3 top = spot_row(S, n0, n0 - 1, v[j], r, half_r, barrier);
@@ -356,7 +361,7 @@ __global__ void build_spot_lines_kernel(Arena A, BuildArgs a) {
 
 enum : int { ST_DOUGLAS = 0, ST_HV0 = 1, ST_HV3 = 2, ST_IMPLICIT = 3 };
 
-// One 8x32 tile of one option. X (the operand of the applies: V, or Y2 in
+// One 16x32 tile of one option. X (the operand of the applies: V, or Y2 in
 // the HV corrector) is staged with a halo of one row above and below, two
 // columns on the left (the A[n1-1, n1-3] corner) and one on the right.
 template <int MODE>
@@ -400,9 +405,9 @@ __global__ void __launch_bounds__(EXPL_THREADS) explicit_kernel(Arena A, const d
 
     double m = 0.0;
     if (mixed && i > 0 && i < n0 - 1 && j > 0 && j < n1 - 1) {
-        const double *c = (MODE == ST_IMPLICIT) ? A.cMi : A.cM;
-        m = c[p] * (A.w0[so + i] * sT[ty][tx] + A.w0[A.SS + so + i] * sT[ty + 1][tx] +
-                    A.w0[2 * A.SS + so + i] * sT[ty + 2][tx]);
+        const double *w0 = (MODE == ST_IMPLICIT) ? A.w0i : A.w0;
+        m = w0[so + i] * sT[ty][tx] + w0[A.SS + so + i] * sT[ty + 1][tx] +
+            w0[2 * A.SS + so + i] * sT[ty + 2][tx];
     }
     const double xc = sX[ty + 1][tx + 2];
     if (MODE == ST_IMPLICIT) {
@@ -428,20 +433,24 @@ __global__ void __launch_bounds__(EXPL_THREADS) explicit_kernel(Arena A, const d
              A.F1v[2 * A.SV + js] * sX[ty + 1][tx + 3];
         if (j == n1 - 1) a1 += A.F1x[o] * sX[ty + 1][tx];
     }
-    const double R = (i == n0 - 1) ? A.R0top[js] : 0.0;
     const double theta = A.theta[o];
+    // T holds F1 x; the spot solve subtracts theta T from its result
     if (MODE == ST_DOUGLAS || MODE == ST_HV0) {
         // Y0 = V + F(V) + R; right-hand side of the spot solve Y0 - theta F0 V
         const double fv = a0 + a1 + m;
         if (MODE == ST_HV0) A.FV[p] = fv;
-        A.W[p] = (xc + R) + fv - theta * a0;
-        A.T[p] = theta * a1;
+        double base = xc + fv;
+        if (i == n0 - 1) base += A.R0top[js];
+        A.W[p] = fma(-theta, a0, base);
+        A.T[p] = a1;
         return;
     }
     // ST_HV3: Y0 - F(V - Y2)/2 = V + R + (F V + F Y2)/2, minus theta F0 Y2
     const double fy = a0 + a1 + m;
-    A.W[p] = (V[p] + R) + 0.5 * (A.FV[p] + fy) - theta * a0;
-    A.T[p] = theta * a1;
+    double vr = V[p];
+    if (i == n0 - 1) vr += A.R0top[js];
+    A.W[p] = fma(-theta, a0, fma(0.5, A.FV[p] + fy, vr));
+    A.T[p] = a1;
 }
 
 // Spot-line solve, one thread per grid column. src -> dst (may alias).
@@ -471,15 +480,16 @@ __global__ void __launch_bounds__(SOLVE_THREADS) spot_solve_kernel(Arena A, cons
         dp = (i == 0) ? rk * L[P + p] : (rk - L[p] * dp) * L[P + p];
         dst[p] = dp;
     }
+    const double th = SUBT ? A.theta[o] : 0.0;
     double x = dp;
     {
         const int64_t p = b + (int64_t)(n0 - 1) * n1;
-        if (SUBT) dst[p] = x - A.T[p];
+        if (SUBT) dst[p] = fma(-th, A.T[p], x);
     }
     for (int i = n0 - 2; i >= 0; --i) {
         const int64_t p = b + (int64_t)i * n1;
         x = dst[p] - L[2 * P + p] * x;
-        dst[p] = SUBT ? x - A.T[p] : x;
+        dst[p] = SUBT ? fma(-th, A.T[p], x) : x;
     }
 }
 
@@ -587,9 +597,9 @@ struct Layout {
     bool smoothing = false, hv = false;
     // byte offsets into the workspace (-1: absent)
     int64_t o_n0, o_n1, o_flags, o_p, o_s, o_v, o_lineS, o_tiles, o_vtasks, o_theta;
-    int64_t o_F0, o_cM, o_w0, o_w1, o_LS, o_R0top, o_F1v, o_F1x, o_F1z, o_LVv, o_foldV, o_LVz,
+    int64_t o_F0, o_w0, o_w1, o_LS, o_R0top, o_F1v, o_F1x, o_F1z, o_LVv, o_foldV, o_LVz,
         o_dirS;
-    int64_t o_cMi, o_RSi, o_LSi, o_LVvi, o_foldVi, o_LVzi;
+    int64_t o_w0i, o_RSi, o_LSi, o_LVvi, o_foldVi, o_LVzi;
     int64_t o_FV, o_W, o_T, o_Y2;
     int64_t bytes = 0;
     std::vector<int64_t> p_off, s_off, v_off;
@@ -634,16 +644,16 @@ static int make_layout(const fdadi_heston_batch_t *b, Layout &L) {
     L.o_p = take(8 * N); L.o_s = take(8 * N); L.o_v = take(8 * N);
     L.o_lineS = take(4 * L.SV); L.o_tiles = take(16 * L.n_tiles);
     L.o_vtasks = take(16 * L.n_vtasks); L.o_theta = take(D * N);
-    L.o_F0 = take(3 * D * L.P); L.o_cM = take(D * L.P);
+    L.o_F0 = take(3 * D * L.P);
     L.o_w0 = take(3 * D * L.SS); L.o_w1 = take(3 * D * L.SV);
     L.o_LS = take(3 * D * L.P); L.o_R0top = take(D * L.SV); L.o_F1v = take(3 * D * L.SV);
     L.o_F1x = take(D * N); L.o_F1z = take(D * N); L.o_LVv = take(3 * D * L.SV);
     L.o_foldV = take(D * N); L.o_LVz = take(D * N); L.o_dirS = take(2 * D * L.SV);
     if (L.smoothing) {
-        L.o_cMi = take(D * L.P); L.o_RSi = take(D * L.SV); L.o_LSi = take(3 * D * L.P);
+        L.o_w0i = take(3 * D * L.SS); L.o_RSi = take(D * L.SV); L.o_LSi = take(3 * D * L.P);
         L.o_LVvi = take(3 * D * L.SV); L.o_foldVi = take(D * N); L.o_LVzi = take(D * N);
     } else {
-        L.o_cMi = L.o_RSi = L.o_LSi = L.o_LVvi = L.o_foldVi = L.o_LVzi = -1;
+        L.o_w0i = L.o_RSi = L.o_LSi = L.o_LVvi = L.o_foldVi = L.o_LVzi = -1;
     }
     L.o_W = take(D * L.P); L.o_T = take(D * L.P);
     if (L.hv) { L.o_FV = take(D * L.P); L.o_Y2 = take(D * L.P); }
@@ -664,11 +674,11 @@ static Arena arena_view(const Layout &L, char *ws) {
     A.tiles = (const int4 *)(ws + L.o_tiles);
     A.vtasks = (const int4 *)(ws + L.o_vtasks);
     A.theta = ptr(L.o_theta);
-    A.F0 = ptr(L.o_F0); A.cM = ptr(L.o_cM); A.w0 = ptr(L.o_w0); A.w1 = ptr(L.o_w1);
+    A.F0 = ptr(L.o_F0); A.w0 = ptr(L.o_w0); A.w1 = ptr(L.o_w1);
     A.LS = ptr(L.o_LS); A.R0top = ptr(L.o_R0top); A.F1v = ptr(L.o_F1v); A.F1x = ptr(L.o_F1x);
     A.F1z = ptr(L.o_F1z); A.LVv = ptr(L.o_LVv); A.foldV = ptr(L.o_foldV); A.LVz = ptr(L.o_LVz);
     A.dirS = ptr(L.o_dirS);
-    A.cMi = ptr(L.o_cMi); A.RSi = ptr(L.o_RSi); A.LSi = ptr(L.o_LSi); A.LVvi = ptr(L.o_LVvi);
+    A.w0i = ptr(L.o_w0i); A.RSi = ptr(L.o_RSi); A.LSi = ptr(L.o_LSi); A.LVvi = ptr(L.o_LVvi);
     A.foldVi = ptr(L.o_foldVi); A.LVzi = ptr(L.o_LVzi);
     A.FV = ptr(L.o_FV); A.W = ptr(L.o_W); A.T = ptr(L.o_T); A.Y2 = ptr(L.o_Y2);
     return A;
