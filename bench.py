@@ -70,6 +70,18 @@ def workload(n_options, seed, nt=200):
                 nS=nS.astype(np.int32), nv=nv.astype(np.int32), nt=nt)
 
 
+def workload_config2():
+    """The large single-instance configuration: rho = -0.7, sigma = 0.5,
+    K in {80, 100, 120} (one option each, run as one batch), 1024 x 512 grid,
+    nt = 1000, HV theta = 1/2 + sqrt(3)/6 after two implicit half-steps."""
+    K = np.array([80.0, 100.0, 120.0])
+    n = K.size
+    return dict(S0=100.0, K=K, T=np.ones(n), r=np.full(n, 0.06), kappa=np.ones(n),
+                theta=np.full(n, 0.04), sigma=np.full(n, 0.5), rho=np.full(n, -0.7),
+                v0=np.full(n, 0.04), nS=np.full(n, 1024, np.int32), nv=np.full(n, 512, np.int32),
+                nt=1000)
+
+
 def subset(w, idx):
     out = dict(w)
     for k, v in w.items():
@@ -281,45 +293,48 @@ def plain_vs_batched(torch, n_batch=2048):
             "price_rel_diff": abs(p_plain - p_batch) / abs(p_plain)}
 
 
-def cpu_baseline(w, n_sample, kind_pref="port"):
-    """Oracle (C restatement, OpenMP over options) or the compat-built
-    reference on this host's cores, on the first n_sample options."""
+def cpu_baseline(w, n_sample, nt_sample=None):
+    """The oracle (C restatement of the reference engine, one OpenMP thread
+    per option) on this host's cores, on n_sample options spread through the
+    workload and, when nt_sample is given, only that many HV steps of each."""
     from oracle import oracle as O
     n = len(w["K"])
     idx = sorted(set(np.linspace(0, n - 1, n_sample).astype(int).tolist()))
     meshes = meshes_for(w, idx)
     V0 = payoffs(w, meshes, idx)
     nt = w["nt"]
-    scheds = [[("implicit", 2, w["T"][k] / nt / 2, 1.0), ("hv", nt - 1, w["T"][k] / nt, HV_THETA)]
+    nrun = nt if nt_sample is None else nt_sample
+    scheds = [[("implicit", 2, w["T"][k] / nt / 2, 1.0), ("hv", nrun - 1, w["T"][k] / nt, HV_THETA)]
               for k in idx]
     cores = os.cpu_count() or 1
     O.build()
     t0 = time.perf_counter()
     O.heston_batch(meshes, params_of(w, idx), V0, scheds, nthreads=cores)
     dt = time.perf_counter() - t0
-    pts = float(sum(int(w["nS"][k]) * int(w["nv"][k]) for k in idx)) * nt
+    pts = float(sum(int(w["nS"][k]) * int(w["nv"][k]) for k in idx)) * nrun
     # the sample's grid-point-step rate, converted to options of the full
     # workload's mean grid size
     mean_pts = float(np.mean(w["nS"].astype(np.int64) * w["nv"])) * nt
     return {"value": pts / dt / mean_pts, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": "%d options evenly spaced through the seeded %d-option workload "
-                      "(%.3g grid-point-steps), all %d cores, %.1f s: %.3g grid-point-steps/s, "
-                      "scaled by the workload's mean grid size" % (len(idx), n, pts, cores, dt,
-                                                                    pts / dt)}
+            "sample": "%d options spread through the %d-option workload, %d of %d time steps "
+                      "(%.3g grid-point-steps), %d cores, %.1f s: %.3g grid-point-steps/s, "
+                      "scaled to the workload's mean option" % (len(idx), n, nrun, nt, pts,
+                                                                 min(cores, len(idx)), dt,
+                                                                 pts / dt)}
 
 
 def run_reference(args, rank, world):
     if rank != 0:
         return 0
-    w = workload(args.options, args.seed)
+    w = workload_config2() if args.workload == "config2" else workload(args.options, args.seed)
     rates = []
     for s in range(args.warmup + args.steps):
-        cb = cpu_baseline(w, args.ref_sample)
+        cb = cpu_baseline(w, args.ref_sample, 20 if args.workload == "config2" else None)
         if s >= args.warmup:
             rates.append(cb["value"])
     value = float(np.mean(rates))
     cb["value"] = value
-    times = [args.options / r for r in rates]
+    times = [len(w["K"]) / r for r in rates]
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": float(np.mean(times)) * 1e3, "higher_is_better": True,
@@ -334,6 +349,13 @@ def run_reference(args, rank, world):
 
 
 def config_block(args, w):
+    if args.workload == "config2":
+        return {"workload": "large single instance x3: K in {80,100,120}, 1024x512, nt=1000, "
+                            "HV theta=1/2+sqrt(3)/6 with Rannacher start, rho=-0.7, sigma=0.5",
+                "options_per_gpu": int(len(w["K"])), "nt": int(w["nt"]),
+                "grid_points": int(np.sum(w["nS"].astype(np.int64) * w["nv"])),
+                "l2": "state arrays larger than L2 (no flush needed)",
+                "parallelism": "dp%d (options sharded, no collective)" % args.gpus}
     return {"workload": "batched Heston calls, uneven grids, HV nt=200 with Rannacher start",
             "options_per_gpu": int(len(w["K"])), "nt": int(w["nt"]),
             "grid_points": int(np.sum(w["nS"].astype(np.int64) * w["nv"])),
@@ -354,6 +376,7 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=32)
     ap.add_argument("--cpu-sample", type=int, default=32)
     ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--workload", default="batch", choices=["batch", "config2"])
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -375,7 +398,8 @@ def main():
     # weak scaling: the seeded workload has args.options options per rank and
     # is partitioned across ranks by work (no data-path collective)
     from fd_adi_gb300.shard import shard_of
-    w_all = workload(args.options * world, args.seed)
+    w_all = (workload_config2() if args.workload == "config2"
+             else workload(args.options * world, args.seed))
     mine = shard_of(w_all["nS"].astype(np.int64) * w_all["nv"], rank, world)
     w = subset(w_all, mine)
     meshes = meshes_for(w)
@@ -485,7 +509,8 @@ def main():
                "stage_ms": {k: round(v[0], 4) for k, v in st.items()},
                "clocks": clk}
         if args.cpu_sample > 0:
-            out["cpu_baseline"] = cpu_baseline(w, args.cpu_sample)
+            out["cpu_baseline"] = cpu_baseline(
+                w, args.cpu_sample, 20 if args.workload == "config2" else None)
         if not args.no_extras:
             out["plain_vs_batched"] = plain_vs_batched(torch)
     if world > 1:
