@@ -456,7 +456,7 @@ __global__ void __launch_bounds__(EXPL_THREADS) explicit_kernel(Arena A, const d
 // Spot-line solve, one thread per grid column. src -> dst (may alias).
 // IMPLICIT: implicit-plan factors and residual. SUBT: write x - T (the next
 // stage's right-hand side) instead of x.
-template <bool IMPLICIT, bool SUBT>
+template <bool IMPLICIT, bool SUBT, int PF>
 __global__ void __launch_bounds__(SOLVE_THREADS) spot_solve_kernel(Arena A, const double *src,
                                                                    double *dst) {
     const int64_t line = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -472,7 +472,7 @@ __global__ void __launch_bounds__(SOLVE_THREADS) spot_solve_kernel(Arena A, cons
     // Rows i+1 .. i+PF are loaded while row i is eliminated: each row's
     // loads are independent of the recurrence, so PF of them stay in flight
     // (src and dst may alias, so the compiler would not hoist them itself).
-    constexpr int PF = 8;
+    // PF = 1 is the plain loop, for batches with enough lines to hide latency.
     double rs[PF], la[PF], li[PF];
 #pragma unroll
     for (int d = 0; d < PF; ++d) {
@@ -725,14 +725,25 @@ static Arena arena_view(const Layout &L, char *ws) {
     return A;
 }
 
+// Launch shape of the spot solve, chosen per batch: with many lines, thread
+// parallelism hides memory latency and the plain loop (fewer registers, more
+// resident threads) is fastest; with few lines (one large grid, small
+// batches) each thread prefetches rows ahead and 32-thread blocks spread the
+// lines over more SMs.
+constexpr int64_t SPOT_MANY_LINES = 150000;
+
 struct Grids {
     unsigned tiles, spot, var;
     int n_vtasks;
+    bool many;       // plain-loop spot solve
+    int spot_threads;
 };
 
 static Grids grids(const Layout &L) {
-    return Grids{(unsigned)L.n_tiles, (unsigned)((L.SV + SOLVE_THREADS - 1) / SOLVE_THREADS),
-                 (unsigned)((L.n_vtasks + VS_WARPS - 1) / VS_WARPS), (int)L.n_vtasks};
+    const bool many = L.SV >= SPOT_MANY_LINES;
+    const int st = many ? SOLVE_THREADS : 32;
+    return Grids{(unsigned)L.n_tiles, (unsigned)((L.SV + st - 1) / st),
+                 (unsigned)((L.n_vtasks + VS_WARPS - 1) / VS_WARPS), (int)L.n_vtasks, many, st};
 }
 
 static void launch_stage(int stage, const Grids &g, const Arena &A, double *V, cudaStream_t st) {
@@ -746,7 +757,9 @@ static void launch_stage(int stage, const Grids &g, const Arena &A, double *V, c
     case FDADI_STAGE_EXPLICIT_IMPLICIT:
         explicit_kernel<ST_IMPLICIT><<<g.tiles, EXPL_THREADS, 0, st>>>(A, V); break;
     case FDADI_STAGE_SPOT_SOLVE:
-        spot_solve_kernel<false, true><<<g.spot, SOLVE_THREADS, 0, st>>>(A, A.W, A.W); break;
+        if (g.many) spot_solve_kernel<false, true, 1><<<g.spot, g.spot_threads, 0, st>>>(A, A.W, A.W);
+        else spot_solve_kernel<false, true, 8><<<g.spot, g.spot_threads, 0, st>>>(A, A.W, A.W);
+        break;
     case FDADI_STAGE_VAR_SOLVE_TO_Y2:
         var_solve_kernel<false><<<g.var, VS_WARPS * 32, 0, st>>>(A, g.n_vtasks, A.W, A.Y2); break;
     case FDADI_STAGE_VAR_SOLVE_TO_V:
@@ -754,7 +767,9 @@ static void launch_stage(int stage, const Grids &g, const Arena &A, double *V, c
     case FDADI_STAGE_VAR_SOLVE_IMPLICIT:
         var_solve_kernel<true><<<g.var, VS_WARPS * 32, 0, st>>>(A, g.n_vtasks, A.W, A.W); break;
     case FDADI_STAGE_SPOT_SOLVE_IMPLICIT:
-        spot_solve_kernel<true, false><<<g.spot, SOLVE_THREADS, 0, st>>>(A, A.W, V); break;
+        if (g.many) spot_solve_kernel<true, false, 1><<<g.spot, g.spot_threads, 0, st>>>(A, A.W, V);
+        else spot_solve_kernel<true, false, 8><<<g.spot, g.spot_threads, 0, st>>>(A, A.W, V);
+        break;
     default: break;
     }
 }
