@@ -469,6 +469,31 @@ __global__ void __launch_bounds__(SOLVE_THREADS) spot_solve_kernel(Arena A, cons
     const int64_t P = A.P, b = A.p_off[o] + j;
     const double *L = IMPLICIT ? A.LSi : A.LS;
     const double gl = A.dirS[js], gh = A.dirS[A.SV + js];
+    if constexpr (PF == 1) {
+        double dp = 0.0;
+        for (int i = 0; i < n0; ++i) {
+            const int64_t p = b + (int64_t)i * n1;
+            double rk;
+            if (i == 0 && slow) rk = gl;
+            else if (i == n0 - 1 && shigh) rk = gh;
+            else rk = src[p];
+            if (IMPLICIT && i == n0 - 1) rk = rk - A.RSi[js];
+            dp = (i == 0) ? rk * L[P + p] : (rk - L[p] * dp) * L[P + p];
+            dst[p] = dp;
+        }
+        const double th = SUBT ? A.theta[o] : 0.0;
+        double x = dp;
+        {
+            const int64_t p = b + (int64_t)(n0 - 1) * n1;
+            if (SUBT) dst[p] = fma(-th, A.T[p], x);
+        }
+        for (int i = n0 - 2; i >= 0; --i) {
+            const int64_t p = b + (int64_t)i * n1;
+            x = dst[p] - L[2 * P + p] * x;
+            dst[p] = SUBT ? fma(-th, A.T[p], x) : x;
+        }
+        return;
+    }
     // Rows i+1 .. i+PF are loaded while row i is eliminated: each row's
     // loads are independent of the recurrence, so PF of them stay in flight
     // (src and dst may alias, so the compiler would not hoist them itself).
