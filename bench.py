@@ -43,6 +43,10 @@ HV_THETA = 0.5 + np.sqrt(3.0) / 6.0
 STAGE_BYTES = {"explicit_hv0": 32, "explicit_hv3": 40, "spot_solve": 24, "var_solve_y2": 16,
                "var_solve_v": 16, "explicit_implicit": 16, "var_solve_implicit": 16,
                "spot_solve_implicit": 16}
+# DRAM bytes per grid point per launch measured by ncu (--set full) on the
+# 256-option cut of the batch workload (profiles/explicit_hv3_batch256.md);
+# traffic grows with the points processed, so a full launch is this x points.
+NCU_TRAFFIC_B_PER_POINT = {"explicit_hv3": 62.4}
 STAGE_FLOPS = {"explicit_hv0": 33.5, "explicit_hv3": 35.5, "spot_solve": 6, "var_solve_y2": 5,
                "var_solve_v": 5, "explicit_implicit": 15.5, "var_solve_implicit": 5,
                "spot_solve_implicit": 5}
@@ -498,7 +502,11 @@ def main():
                "gpu_launches": int(launches),
                "grid_point_steps_per_s": pts_steps * world / (ms * 1e-3),
                "roofline": {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": hbm_peak,
-                            "unit": "GB/s", "frac": ach / hbm_peak, "traffic": None,
+                            "unit": "GB/s", "frac": ach / hbm_peak,
+                            "traffic": (NCU_TRAFFIC_B_PER_POINT[dom] * P
+                                        if dom in NCU_TRAFFIC_B_PER_POINT else None),
+                            "traffic_source": "ncu dram__bytes_read+write per point (256-option "
+                                              "capture) x points of this launch",
                             "peak_source": peak_src,
                             "bytes_per_point": STAGE_BYTES[dom],
                             "avg_launch_ms": avg_ms, "launches": st[dom][1]},
