@@ -54,6 +54,19 @@ class HestonBatch(ctypes.Structure):
                 ("barrier", ctypes.c_void_p)]
 
 
+class Gemm(ctypes.Structure):
+    """fdadi_gemm_t"""
+    _fields_ = [("A", ctypes.c_void_p), ("lda", ctypes.c_int64), ("strideA", ctypes.c_int64),
+                ("B", ctypes.c_void_p), ("ldb", ctypes.c_int64), ("strideB", ctypes.c_int64),
+                ("bias", ctypes.c_void_p), ("strideBias", ctypes.c_int64),
+                ("aux", ctypes.c_void_p), ("ldaux", ctypes.c_int64), ("strideAux", ctypes.c_int64),
+                ("out_f32", ctypes.c_void_p), ("ldo", ctypes.c_int64), ("strideO", ctypes.c_int64),
+                ("out_bf16", ctypes.c_void_p), ("ldh", ctypes.c_int64), ("strideH", ctypes.c_int64),
+                ("M", ctypes.c_int32), ("N", ctypes.c_int32), ("K", ctypes.c_int32),
+                ("act", ctypes.c_int32), ("problems", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("status", ctypes.c_void_p)]
+
+
 # name -> (restype, argtypes); every symbol include/fdadi.h declares
 SIGNATURES = {
     "fdadi_version": (ctypes.c_int, []),
@@ -89,6 +102,24 @@ SIGNATURES = {
     "fdadi_heston_stage": (ctypes.c_int, [ctypes.POINTER(HestonBatch), ctypes.c_void_p,
                                           ctypes.c_int64, ctypes.c_void_p, ctypes.c_int32,
                                           ctypes.c_void_p]),
+    "fdadi_mlp_gemm": (ctypes.c_int, [ctypes.POINTER(Gemm), ctypes.c_void_p]),
+    "fdadi_transpose_bf16": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
+                                            ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
+                                            ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                            ctypes.c_void_p]),
+    "fdadi_mlp_mse": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
+                                     ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
+                                     ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
+                                     ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                     ctypes.c_void_p, ctypes.c_void_p]),
+    "fdadi_mlp_colsum": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
+                                        ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32,
+                                        ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p]),
+    "fdadi_mlp_adam": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                      ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32,
+                                      ctypes.c_int32, ctypes.c_float, ctypes.c_float,
+                                      ctypes.c_float, ctypes.c_float, ctypes.c_int32,
+                                      ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "fdadi_fp64_probe": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
                                         ctypes.c_int32, ctypes.POINTER(ctypes.c_double),
                                         ctypes.c_void_p]),

@@ -1,0 +1,361 @@
+// BF16 tensor-core kernels of the pricing surrogate (5th-generation tensor
+// cores: tcgen05.mma with operands in shared memory and the FP32 accumulator
+// in tensor memory).
+//
+// One GEMM form serves forward, backward and the weight gradients:
+//     C[M, N] = A[M, K] * B[N, K]^T     (A, B bf16, K contiguous; C fp32)
+// with M a multiple of 128, N in {16, 32, ..., 256}, K a multiple of 16, and a
+// fused epilogue (bias, SiLU, multiplication by SiLU'(aux), fp32 and/or bf16
+// stores). Transposed operands are produced by a separate transpose kernel.
+//
+// A CTA (4 warps) owns one 128 x N tile. For each K chunk of 64 it stages the
+// A and B chunks in shared memory in the canonical no-swizzle K-major layout
+// (8-row x 16-byte core matrices: core matrices adjacent in K are 128 bytes
+// apart, 8-row groups are chunk/8 * 128 bytes apart), one elected thread
+// issues the tcgen05.mma instructions (K = 16 each) accumulating into tensor
+// memory and commits them to an mbarrier; every wait on that mbarrier is
+// bounded and sets the status word instead of hanging. The epilogue reads the
+// accumulator rows with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31).
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+#include "fdadi_internal.cuh"
+
+namespace fdadi {
+
+typedef __nv_bfloat16 bf16;
+
+constexpr int GM_BM = 128;          // tile rows (UMMA M)
+constexpr int GM_BK = 64;           // K chunk staged per MMA round
+constexpr int GM_THREADS = 128;
+constexpr int GM_A_BYTES = GM_BM * GM_BK * 2;      // 16 KB
+constexpr int GM_B_BYTES = 256 * GM_BK * 2;        // 32 KB (N <= 256)
+constexpr int GM_SMEM = 100 * 1024; // requested per CTA: two CTAs per SM, so two
+                                    // 256-column accumulators fit in TMEM (512)
+constexpr long long GM_WAIT_CYCLES = 4000000000LL;  // ~2 s at 2 GHz
+
+struct GemmArgs {
+    const bf16 *A; int64_t lda, strideA;
+    const bf16 *B; int64_t ldb, strideB;
+    const float *bias; int64_t strideBias;
+    const float *aux; int64_t ldaux, strideAux;
+    float *out_f32; int64_t ldo, strideO;
+    bf16 *out_bf16; int64_t ldh, strideH;
+    int M, N, K;
+    int act;          // 0: none, 1: SiLU, 2: multiply by SiLU'(aux)
+    int *status;      // set to 1 if an mbarrier wait timed out
+};
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// tcgen05 shared-memory matrix descriptor: start address, leading (K) byte
+// offset, stride (8-row group) byte offset, descriptor version 1, no swizzle.
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, N >> 3 at bit 17, M >> 4 at bit 24.
+__device__ __forceinline__ uint32_t umma_idesc(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
+           ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ float silu(float x) { return x / (1.0f + expf(-x)); }
+__device__ __forceinline__ float dsilu(float x) {
+    const float s = 1.0f / (1.0f + expf(-x));
+    return s * (1.0f + x * (1.0f - s));
+}
+
+__global__ void __launch_bounds__(GM_THREADS) umma_gemm_kernel(GemmArgs g) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned char *sA = smem;
+    unsigned char *sB = smem + GM_A_BYTES;
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + GM_A_BYTES + GM_B_BYTES);
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + GM_A_BYTES + GM_B_BYTES + 8);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int prob = blockIdx.y;
+    const int m0 = blockIdx.x * GM_BM;
+    const bf16 *A = g.A + prob * g.strideA;
+    const bf16 *B = g.B + prob * g.strideB;
+    const int N = g.N, K = g.K;
+    const uint32_t ncols = N <= 32 ? 32 : N <= 64 ? 64 : N <= 128 ? 128 : 256;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     ::"r"(smem_addr(tslot)), "r"(ncols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(mbar)));
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = *tslot;
+    const uint32_t idesc = umma_idesc(GM_BM, N);
+
+    bool ok = true;
+    uint32_t phase = 0;
+    for (int k0 = 0; k0 < K; k0 += GM_BK) {
+        const int kw = min(GM_BK, K - k0);     // multiple of 16
+        const int kc = kw >> 3;                // 16-byte core-matrix columns
+        const uint32_t sbo = (uint32_t)kc * 128;
+        // stage A (128 rows) and B (N rows): 16-byte chunk (row r, column c)
+        // goes to (r / 8) * sbo + c * 128 + (r % 8) * 16
+        for (int q = tid; q < GM_BM * kc; q += GM_THREADS) {
+            const int r = q / kc, c = q - r * kc;
+            const uint4 v = *reinterpret_cast<const uint4 *>(A + (int64_t)(m0 + r) * g.lda + k0 + c * 8);
+            *reinterpret_cast<uint4 *>(sA + (r >> 3) * sbo + c * 128 + (r & 7) * 16) = v;
+        }
+        for (int q = tid; q < N * kc; q += GM_THREADS) {
+            const int r = q / kc, c = q - r * kc;
+            const uint4 v = *reinterpret_cast<const uint4 *>(B + (int64_t)r * g.ldb + k0 + c * 8);
+            *reinterpret_cast<uint4 *>(sB + (r >> 3) * sbo + c * 128 + (r & 7) * 16) = v;
+        }
+        asm volatile("fence.proxy.async.shared::cta;");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            for (int s = 0; s < (kw >> 4); ++s) {
+                const uint64_t ad = umma_desc(smem_addr(sA) + s * 256, 128, sbo);
+                const uint64_t bd = umma_desc(smem_addr(sB) + s * 256, 128, sbo);
+                const uint32_t acc = (k0 > 0 || s > 0) ? 1u : 0u;
+                asm volatile(
+                    "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+                    ::"r"(tmem), "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                         ::"r"(smem_addr(mbar)));
+        }
+        // bounded wait for the MMAs of this chunk (they read sA/sB)
+        const long long t0 = clock64();
+        uint32_t done = 0;
+        while (!done) {
+            asm volatile(
+                "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                "selp.u32 %0, 1, 0, p;\n}\n"
+                : "=r"(done) : "r"(smem_addr(mbar)), "r"(phase));
+            if (!done && clock64() - t0 > GM_WAIT_CYCLES) {
+                ok = false;
+                break;
+            }
+        }
+        phase ^= 1u;
+        // every thread reaches this barrier, timed out or not, so the
+        // decision to stop is the same for the whole block
+        if (!__syncthreads_and(ok ? 1 : 0)) {
+            ok = false;
+            break;
+        }
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (!ok) {
+        if (tid == 0 && g.status) atomicExch(g.status, 1);
+    } else {
+        const int m = m0 + warp * 32 + lane;
+        const float *bias = g.bias ? g.bias + prob * g.strideBias : nullptr;
+        const float *aux = g.aux ? g.aux + prob * g.strideAux + (int64_t)m * g.ldaux : nullptr;
+        float *of = g.out_f32 ? g.out_f32 + prob * g.strideO + (int64_t)m * g.ldo : nullptr;
+        bf16 *oh = g.out_bf16 ? g.out_bf16 + prob * g.strideH + (int64_t)m * g.ldh : nullptr;
+        for (int c0 = 0; c0 < N; c0 += 8) {
+            uint32_t r[8];
+            const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+                  "=r"(r[6]), "=r"(r[7])
+                : "r"(taddr));
+            asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+                float x = __uint_as_float(r[e]);
+                const int n = c0 + e;
+                if (bias) x += bias[n];
+                if (of) of[n] = x;
+                if (g.act == 1) x = silu(x);
+                else if (g.act == 2) x *= dsilu(aux[n]);
+                if (oh) oh[n] = __float2bfloat16(x);
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols));
+    }
+}
+
+// out[c][r] = in[r][c] for an R x C bf16 matrix (per problem: blockIdx.z).
+__global__ void transpose_bf16_kernel(const bf16 *in, int64_t ldi, int64_t stride_in, bf16 *out,
+                                      int64_t ldo, int64_t stride_out, int R, int C) {
+    __shared__ bf16 t[32][33];
+    const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+    in += blockIdx.z * stride_in;
+    out += blockIdx.z * stride_out;
+    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+        const int r = r0 + k, c = c0 + threadIdx.x;
+        t[k][threadIdx.x] = (r < R && c < C) ? in[(int64_t)r * ldi + c] : __float2bfloat16(0.0f);
+    }
+    __syncthreads();
+    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+        const int c = c0 + k, r = r0 + threadIdx.x;
+        if (c < C && r < R) out[(int64_t)c * ldo + r] = t[threadIdx.x][k];
+    }
+}
+
+// Weighted squared error on the first `nout` columns of pred [M][ldp]
+// (fp32, per problem) against target [M][nout]; writes the bf16 gradient
+// d pred = 2 w (pred - target) / M into grad [M][ldg] (zero elsewhere) and
+// accumulates the loss per problem.
+__global__ void mse_kernel(const float *pred, int64_t ldp, int64_t stride_p, const float *target,
+                           const float *w, int nout, bf16 *grad, int64_t ldg, int64_t stride_g,
+                           int M, int ncols, double *loss) {
+    const int prob = blockIdx.y;
+    pred += prob * stride_p;
+    grad += prob * stride_g;
+    double acc = 0.0;
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x) {
+        for (int c = 0; c < ncols; ++c) {
+            float gval = 0.0f;
+            if (c < nout) {
+                const float d = pred[(int64_t)m * ldp + c] - target[(int64_t)m * nout + c];
+                acc += (double)(w[c] * d * d);
+                gval = 2.0f * w[c] * d / (float)M;
+            }
+            grad[(int64_t)m * ldg + c] = __float2bfloat16(gval);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(&loss[prob], acc / M);
+}
+
+// db[n] = sum_m dy[m][n] (bias gradient), per problem.
+__global__ void colsum_kernel(const bf16 *dy, int64_t ld, int64_t stride, float *db,
+                              int64_t stride_db, int M, int N) {
+    const int prob = blockIdx.y;
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= N) return;
+    dy += prob * stride;
+    float s = 0.0f;
+    for (int m = 0; m < M; ++m) s += __bfloat162float(dy[(int64_t)m * ld + n]);
+    db[prob * stride_db + n] = s;
+}
+
+// Adam on FP32 master parameters; also refreshes the bf16 working copies:
+// W [rows][cols] and, if wt is given, W^T [cols][rows].
+__global__ void adam_kernel(float *p, const float *gr, float *m1, float *m2, int64_t n, int cols,
+                            float lr, float b1, float b2, float eps, float c1, float c2,
+                            bf16 *w, bf16 *wt, int rows) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        const float gk = gr[k];
+        const float a = b1 * m1[k] + (1.0f - b1) * gk;
+        const float b = b2 * m2[k] + (1.0f - b2) * gk * gk;
+        m1[k] = a;
+        m2[k] = b;
+        const float upd = lr * (a / c1) / (sqrtf(b / c2) + eps);
+        const float x = p[k] - upd;
+        p[k] = x;
+        if (w) w[k] = __float2bfloat16(x);
+        if (wt) {
+            const int64_t r = k / cols, c = k - r * cols;
+            wt[c * rows + r] = __float2bfloat16(x);
+        }
+    }
+}
+
+}  // namespace fdadi
+
+using namespace fdadi;
+
+extern "C" {
+
+int fdadi_mlp_gemm(const fdadi_gemm_t *a, void *stream) {
+    FDADI_REQUIRE(a && a->A && a->B, "null GEMM operand");
+    FDADI_REQUIRE(a->M > 0 && a->M % 128 == 0, "GEMM M must be a positive multiple of 128 (%d)", a->M);
+    FDADI_REQUIRE(a->N >= 16 && a->N <= 256 && a->N % 16 == 0, "GEMM N must be 16..256, step 16 (%d)", a->N);
+    FDADI_REQUIRE(a->K >= 16 && a->K % 16 == 0, "GEMM K must be a positive multiple of 16 (%d)", a->K);
+    FDADI_REQUIRE(a->lda % 8 == 0 && a->ldb % 8 == 0 && a->lda >= a->K && a->ldb >= a->K,
+                  "GEMM leading dimensions must be multiples of 8 elements and >= K");
+    FDADI_REQUIRE(((uintptr_t)a->A % 16 == 0) && ((uintptr_t)a->B % 16 == 0) &&
+                      a->strideA % 8 == 0 && a->strideB % 8 == 0,
+                  "GEMM operands must be 16-byte aligned");
+    FDADI_REQUIRE(a->act == 0 || a->act == 1 || (a->act == 2 && a->aux), "bad GEMM epilogue");
+    FDADI_REQUIRE(a->problems >= 1, "GEMM needs at least one problem");
+    static bool attr[64] = {false};
+    int dev = 0;
+    FDADI_CUDA(cudaGetDevice(&dev));
+    FDADI_REQUIRE(dev >= 0 && dev < 64, "device ordinal out of range");
+    if (!attr[dev]) {
+        FDADI_CUDA(cudaFuncSetAttribute(umma_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        GM_SMEM));
+        attr[dev] = true;
+    }
+    GemmArgs g{(const bf16 *)a->A, a->lda, a->strideA, (const bf16 *)a->B, a->ldb, a->strideB,
+               a->bias, a->strideBias, a->aux, a->ldaux, a->strideAux, a->out_f32, a->ldo,
+               a->strideO, (bf16 *)a->out_bf16, a->ldh, a->strideH, a->M, a->N, a->K, a->act,
+               a->status};
+    dim3 grid(a->M / 128, a->problems);
+    umma_gemm_kernel<<<grid, GM_THREADS, GM_SMEM, as_stream(stream)>>>(g);
+    FDADI_CHECK_LAUNCH();
+    return FDADI_OK;
+}
+
+int fdadi_transpose_bf16(const void *in, int64_t ldi, int64_t stride_in, void *out, int64_t ldo,
+                         int64_t stride_out, int32_t rows, int32_t cols, int32_t problems,
+                         void *stream) {
+    FDADI_REQUIRE(in && out && rows > 0 && cols > 0 && problems > 0, "bad transpose arguments");
+    dim3 grid((cols + 31) / 32, (rows + 31) / 32, problems), block(32, 8);
+    transpose_bf16_kernel<<<grid, block, 0, as_stream(stream)>>>(
+        (const bf16 *)in, ldi, stride_in, (bf16 *)out, ldo, stride_out, rows, cols);
+    FDADI_CHECK_LAUNCH();
+    return FDADI_OK;
+}
+
+int fdadi_mlp_mse(const float *pred, int64_t ldp, int64_t stride_p, const float *target,
+                  const float *weights, int32_t nout, void *grad, int64_t ldg, int64_t stride_g,
+                  int32_t M, int32_t ncols, int32_t problems, double *loss, void *stream) {
+    FDADI_REQUIRE(pred && target && weights && grad && loss && M > 0 && nout <= ncols,
+                  "bad loss arguments");
+    dim3 grid((M + 255) / 256 < 1024 ? (M + 255) / 256 : 1024, problems);
+    mse_kernel<<<grid, 256, 0, as_stream(stream)>>>(pred, ldp, stride_p, target, weights, nout,
+                                                    (bf16 *)grad, ldg, stride_g, M, ncols, loss);
+    FDADI_CHECK_LAUNCH();
+    return FDADI_OK;
+}
+
+int fdadi_mlp_colsum(const void *dy, int64_t ld, int64_t stride, float *db, int64_t stride_db,
+                     int32_t M, int32_t N, int32_t problems, void *stream) {
+    FDADI_REQUIRE(dy && db && M > 0 && N > 0, "bad column-sum arguments");
+    dim3 grid((N + 127) / 128, problems);
+    colsum_kernel<<<grid, 128, 0, as_stream(stream)>>>((const bf16 *)dy, ld, stride, db, stride_db,
+                                                       M, N);
+    FDADI_CHECK_LAUNCH();
+    return FDADI_OK;
+}
+
+int fdadi_mlp_adam(float *p, const float *g, float *m1, float *m2, int64_t n, int32_t rows,
+                   int32_t cols, float lr, float b1, float b2, float eps, int32_t step, void *w,
+                   void *wt, void *stream) {
+    FDADI_REQUIRE(p && g && m1 && m2 && n > 0 && step >= 1, "bad Adam arguments");
+    FDADI_REQUIRE(!wt || (int64_t)rows * cols == n, "transposed copy needs rows * cols == n");
+    const float c1 = 1.0f - powf(b1, (float)step), c2 = 1.0f - powf(b2, (float)step);
+    adam_kernel<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(p, g, m1, m2, n, cols > 0 ? cols : 1,
+                                                                 lr, b1, b2, eps, c1, c2,
+                                                                 (bf16 *)w, (bf16 *)wt, rows);
+    FDADI_CHECK_LAUNCH();
+    return FDADI_OK;
+}
+
+}  // extern "C"

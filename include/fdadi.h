@@ -229,6 +229,55 @@ int fdadi_heston_stage(const fdadi_heston_batch_t *batch, void *workspace,
 int fdadi_fp64_probe(double *out, int32_t blocks, int32_t threads, int32_t iters,
                      double *flops, void *stream);
 
+/* ------------------------------------------------------------------------ */
+/* Pricing surrogate: BF16 tensor-core MLP kernels (no reference            */
+/* counterpart; the reference prices every option with ADI).                */
+/* ------------------------------------------------------------------------ */
+
+/* C[M,N] = A[M,K] * B[N,K]^T on 5th-generation tensor cores (tcgen05.mma,
+ * accumulator in tensor memory), FP32 accumulation, for `problems`
+ * independent problems (operand p at base + p * stride). A and B are bf16 with
+ * K contiguous; M % 128 == 0, N in 16..256 step 16, K % 16 == 0, leading
+ * dimensions multiples of 8 elements, 16-byte aligned bases. Epilogue per
+ * element: x = acc (+ bias[n]); out_f32 = x; act 1: x = SiLU(x), act 2:
+ * x *= SiLU'(aux[m][n]); out_bf16 = bf16(x). *status is set to 1 if a
+ * tensor-core completion wait timed out (the kernel then returns without
+ * writing). */
+typedef struct fdadi_gemm {
+    const void *A; int64_t lda, strideA;
+    const void *B; int64_t ldb, strideB;
+    const float *bias; int64_t strideBias;
+    const float *aux; int64_t ldaux, strideAux;
+    float *out_f32; int64_t ldo, strideO;
+    void *out_bf16; int64_t ldh, strideH;
+    int32_t M, N, K, act, problems, reserved;
+    int32_t *status;
+} fdadi_gemm_t;
+int fdadi_mlp_gemm(const fdadi_gemm_t *gemm, void *stream);
+
+/* out[c][r] = in[r][c] (bf16), per problem. */
+int fdadi_transpose_bf16(const void *in, int64_t ldi, int64_t stride_in, void *out, int64_t ldo,
+                         int64_t stride_out, int32_t rows, int32_t cols, int32_t problems,
+                         void *stream);
+
+/* Weighted mean squared error of pred[:, :nout] (fp32) against target
+ * [M][nout]; writes the bf16 gradient into grad[M][ncols] (zero beyond nout)
+ * and adds the loss of problem p to loss[p]. */
+int fdadi_mlp_mse(const float *pred, int64_t ldp, int64_t stride_p, const float *target,
+                  const float *weights, int32_t nout, void *grad, int64_t ldg, int64_t stride_g,
+                  int32_t M, int32_t ncols, int32_t problems, double *loss, void *stream);
+
+/* db[n] = sum_m dy[m][n] (bf16 dy, fp32 db), per problem. */
+int fdadi_mlp_colsum(const void *dy, int64_t ld, int64_t stride, float *db, int64_t stride_db,
+                     int32_t M, int32_t N, int32_t problems, void *stream);
+
+/* One Adam step on FP32 master parameters p (n values; a rows x cols matrix
+ * when w/wt are given) with gradient g and moments m1, m2; refreshes the bf16
+ * copies w (same layout) and wt (transposed) when non-NULL. */
+int fdadi_mlp_adam(float *p, const float *g, float *m1, float *m2, int64_t n, int32_t rows,
+                   int32_t cols, float lr, float b1, float b2, float eps, int32_t step, void *w,
+                   void *wt, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
