@@ -492,67 +492,67 @@ __global__ void __launch_bounds__(SOLVE_THREADS) spot_solve_kernel(Arena A, cons
             x = dst[p] - L[2 * P + p] * x;
             dst[p] = SUBT ? fma(-th, A.T[p], x) : x;
         }
-        return;
-    }
-    // Rows i+1 .. i+PF are loaded while row i is eliminated: each row's
-    // loads are independent of the recurrence, so PF of them stay in flight
-    // (src and dst may alias, so the compiler would not hoist them itself).
-    // PF = 1 is the plain loop, for batches with enough lines to hide latency.
-    double rs[PF], la[PF], li[PF];
-#pragma unroll
-    for (int d = 0; d < PF; ++d) {
-        if (d < n0) {
-            const int64_t p = b + (int64_t)d * n1;
-            rs[d] = src[p]; la[d] = L[p]; li[d] = L[P + p];
-        }
-    }
-    double dp = 0.0;
-    for (int i0 = 0; i0 < n0; i0 += PF) {
-#pragma unroll
+    } else {
+        // Rows i+1 .. i+PF are loaded while row i is eliminated: each row's
+        // loads are independent of the recurrence, so PF of them stay in flight
+        // (src and dst may alias, so the compiler would not hoist them itself).
+        // PF = 1 is the plain loop, for batches with enough lines to hide latency.
+        double rs[PF], la[PF], li[PF];
+    #pragma unroll
         for (int d = 0; d < PF; ++d) {
-            const int i = i0 + d;
-            if (i < n0) {
-                const int64_t p = b + (int64_t)i * n1;
-                double rk = rs[d];
-                if (i == 0 && slow) rk = gl;
-                else if (i == n0 - 1 && shigh) rk = gh;
-                if (IMPLICIT && i == n0 - 1) rk = rk - A.RSi[js];
-                dp = (i == 0) ? rk * li[d] : (rk - la[d] * dp) * li[d];
-                dst[p] = dp;
-                if (i + PF < n0) {
-                    const int64_t q = p + (int64_t)PF * n1;
-                    rs[d] = src[q]; la[d] = L[q]; li[d] = L[P + q];
+            if (d < n0) {
+                const int64_t p = b + (int64_t)d * n1;
+                rs[d] = src[p]; la[d] = L[p]; li[d] = L[P + p];
+            }
+        }
+        double dp = 0.0;
+        for (int i0 = 0; i0 < n0; i0 += PF) {
+    #pragma unroll
+            for (int d = 0; d < PF; ++d) {
+                const int i = i0 + d;
+                if (i < n0) {
+                    const int64_t p = b + (int64_t)i * n1;
+                    double rk = rs[d];
+                    if (i == 0 && slow) rk = gl;
+                    else if (i == n0 - 1 && shigh) rk = gh;
+                    if (IMPLICIT && i == n0 - 1) rk = rk - A.RSi[js];
+                    dp = (i == 0) ? rk * li[d] : (rk - la[d] * dp) * li[d];
+                    dst[p] = dp;
+                    if (i + PF < n0) {
+                        const int64_t q = p + (int64_t)PF * n1;
+                        rs[d] = src[q]; la[d] = L[q]; li[d] = L[P + q];
+                    }
                 }
             }
         }
-    }
-    // back substitution, bottom to top, with the same prefetch ring
-    const double th = SUBT ? A.theta[o] : 0.0;
-    double ds[PF], cs[PF], ts[PF];
-#pragma unroll
-    for (int d = 0; d < PF; ++d) {
-        const int i = n0 - 2 - d;
-        if (i >= 0) {
-            const int64_t p = b + (int64_t)i * n1;
-            ds[d] = dst[p]; cs[d] = L[2 * P + p]; ts[d] = SUBT ? A.T[p] : 0.0;
-        }
-    }
-    double x = dp;
-    if (SUBT) {
-        const int64_t p = b + (int64_t)(n0 - 1) * n1;
-        dst[p] = fma(-th, A.T[p], x);
-    }
-    for (int k0 = 0; k0 < n0 - 1; k0 += PF) {
-#pragma unroll
+        // back substitution, bottom to top, with the same prefetch ring
+        const double th = SUBT ? A.theta[o] : 0.0;
+        double ds[PF], cs[PF], ts[PF];
+    #pragma unroll
         for (int d = 0; d < PF; ++d) {
-            const int i = n0 - 2 - (k0 + d);
+            const int i = n0 - 2 - d;
             if (i >= 0) {
                 const int64_t p = b + (int64_t)i * n1;
-                x = ds[d] - cs[d] * x;
-                dst[p] = SUBT ? fma(-th, ts[d], x) : x;
-                if (i - PF >= 0) {
-                    const int64_t q = p - (int64_t)PF * n1;
-                    ds[d] = dst[q]; cs[d] = L[2 * P + q]; ts[d] = SUBT ? A.T[q] : 0.0;
+                ds[d] = dst[p]; cs[d] = L[2 * P + p]; ts[d] = SUBT ? A.T[p] : 0.0;
+            }
+        }
+        double x = dp;
+        if (SUBT) {
+            const int64_t p = b + (int64_t)(n0 - 1) * n1;
+            dst[p] = fma(-th, A.T[p], x);
+        }
+        for (int k0 = 0; k0 < n0 - 1; k0 += PF) {
+    #pragma unroll
+            for (int d = 0; d < PF; ++d) {
+                const int i = n0 - 2 - (k0 + d);
+                if (i >= 0) {
+                    const int64_t p = b + (int64_t)i * n1;
+                    x = ds[d] - cs[d] * x;
+                    dst[p] = SUBT ? fma(-th, ts[d], x) : x;
+                    if (i - PF >= 0) {
+                        const int64_t q = p - (int64_t)PF * n1;
+                        ds[d] = dst[q]; cs[d] = L[2 * P + q]; ts[d] = SUBT ? A.T[q] : 0.0;
+                    }
                 }
             }
         }

@@ -275,6 +275,65 @@ __global__ void adam_kernel(float *p, const float *gr, float *m1, float *m2, int
     }
 }
 
+// Surrogate front end, one query per thread. Query q = (S0, K, T, r, kappa,
+// theta, sigma, rho, v0) [9 doubles]; features f = (S0/K, T, r, kappa, theta,
+// sigma, rho, v0) mapped to [-1, 1] by the training box (lo, hi) as bf16
+// inputs (8 of 16 columns; the rest zero); a Black-Scholes control variate at
+// the expected mean variance vbar = theta + (v0 - theta)(1 - e^{-kappa T})/(kappa T):
+// base = (price / K, delta); inbox = every feature inside the box.
+__global__ void featurize_kernel(const double *q, int M, const double *lo, const double *hi,
+                                 bf16 *X, double *base, int *inbox) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= M) return;
+    const double *p = q + 9 * (int64_t)m;
+    const double S = p[0], K = p[1], T = p[2], r = p[3], kap = p[4], th = p[5], v0 = p[8];
+    const double f[8] = {S / K, T, r, kap, th, p[6], p[7], v0};
+    int in = 1;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        if (!(f[k] >= lo[k] && f[k] <= hi[k])) in = 0;
+        X[(int64_t)m * 16 + k] = __float2bfloat16((float)(2.0 * (f[k] - lo[k]) / (hi[k] - lo[k]) - 1.0));
+    }
+#pragma unroll
+    for (int k = 8; k < 16; ++k) X[(int64_t)m * 16 + k] = __float2bfloat16(0.0f);
+    inbox[m] = in;
+    const double kt = kap * T;
+    const double vbar = kt > 1e-12 ? th + (v0 - th) * (1.0 - exp(-kt)) / kt : v0;
+    const double sv = sqrt(fmax(vbar, 1e-12) * T);
+    const double d1 = (log(S / K) + r * T) / sv + 0.5 * sv, d2 = d1 - sv;
+    const double n1 = 0.5 * erfc(-d1 * 0.7071067811865476), n2 = 0.5 * erfc(-d2 * 0.7071067811865476);
+    base[2 * (int64_t)m] = (S / K) * n1 - exp(-r * T) * n2;
+    base[2 * (int64_t)m + 1] = n1;
+}
+
+// Ensemble read-out: member outputs y[p][m][0..1] (scaled residuals) ->
+// price = K (base0 + mean y0 / s0), delta = base1 + mean y1 / s1, spread =
+// max - min of the members' prices; fallback when out of the box or spread
+// > tol K.
+__global__ void combine_kernel(const float *y, int64_t ldy, int64_t stride, int P, int M,
+                               const double *q, const double *base, const int *inbox, double s0,
+                               double s1, double tol, double *price, double *delta,
+                               double *spread, int *fallback, int *count) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= M) return;
+    const double K = q[9 * (int64_t)m + 1];
+    double sp = 0.0, sd = 0.0, mn = 1e300, mx = -1e300;
+    for (int k = 0; k < P; ++k) {
+        const float *row = y + k * stride + (int64_t)m * ldy;
+        const double pk = K * (base[2 * (int64_t)m] + (double)row[0] / s0);
+        sp += pk;
+        sd += base[2 * (int64_t)m + 1] + (double)row[1] / s1;
+        mn = fmin(mn, pk);
+        mx = fmax(mx, pk);
+    }
+    price[m] = sp / P;
+    delta[m] = sd / P;
+    spread[m] = mx - mn;
+    const int fb = (!inbox[m]) || (mx - mn > tol * K);
+    fallback[m] = fb;
+    if (fb) atomicAdd(count, 1);
+}
+
 }  // namespace fdadi
 
 using namespace fdadi;
@@ -354,6 +413,29 @@ int fdadi_mlp_adam(float *p, const float *g, float *m1, float *m2, int64_t n, in
     adam_kernel<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(p, g, m1, m2, n, cols > 0 ? cols : 1,
                                                                  lr, b1, b2, eps, c1, c2,
                                                                  (bf16 *)w, (bf16 *)wt, rows);
+    FDADI_CHECK_LAUNCH();
+    return FDADI_OK;
+}
+
+int fdadi_mlp_featurize(const double *queries, int32_t M, const double *lo, const double *hi,
+                        void *X, double *base, int32_t *inbox, void *stream) {
+    FDADI_REQUIRE(queries && lo && hi && X && base && inbox && M > 0, "bad featurize arguments");
+    featurize_kernel<<<(M + 255) / 256, 256, 0, as_stream(stream)>>>(queries, M, lo, hi, (bf16 *)X,
+                                                                    base, inbox);
+    FDADI_CHECK_LAUNCH();
+    return FDADI_OK;
+}
+
+int fdadi_mlp_combine(const float *y, int64_t ldy, int64_t stride, int32_t problems, int32_t M,
+                      const double *queries, const double *base, const int32_t *inbox, double s0,
+                      double s1, double tol, double *price, double *delta, double *spread,
+                      int32_t *fallback, int32_t *count, void *stream) {
+    FDADI_REQUIRE(y && queries && base && inbox && price && delta && spread && fallback && count &&
+                      M > 0 && problems > 0,
+                  "bad combine arguments");
+    combine_kernel<<<(M + 255) / 256, 256, 0, as_stream(stream)>>>(
+        y, ldy, stride, problems, M, queries, base, inbox, s0, s1, tol, price, delta, spread,
+        fallback, count);
     FDADI_CHECK_LAUNCH();
     return FDADI_OK;
 }

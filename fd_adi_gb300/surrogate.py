@@ -1,0 +1,316 @@
+"""Learned pricing surrogate with FP64 ADI fallback.
+
+A 4-member ensemble of MLPs 8 -> 256 -> 256 -> 256 -> 256 -> 2 (SiLU) maps the
+Heston parameters (S0/K, T, r, kappa, theta, sigma, rho, v0) to price/K and
+delta. Each member learns the residual over a Black-Scholes control variate
+evaluated at the expected mean variance, which leaves the network a small,
+smooth correction. Weights and activations are bf16, accumulation and
+pre-activations fp32, master weights fp32 (Adam). Every layer of forward,
+backward and the weight update runs in libfdadi.so (tcgen05 tensor-core GEMMs
+with fused epilogues, include/fdadi.h); the four members are batched in every
+launch. Training data come from the batched FP64 ADI engine. Queries outside
+the training box, or where the members disagree by more than a tolerance, are
+re-priced by that engine.
+
+There is no counterpart in the reference, which prices every option by ADI.
+"""
+import ctypes
+import math
+
+import numpy as np
+import torch
+
+from . import _lib
+from . import mesh as _mesh
+
+# training box: features S0/K, T, r, kappa, theta, sigma, rho, v0
+BOX_LO = np.array([1 / 1.3, 0.1, 0.0, 0.5, 0.01, 0.1, -0.9, 0.01])
+BOX_HI = np.array([1 / 0.7, 2.0, 0.08, 5.0, 0.16, 1.0, 0.0, 0.16])
+HV_THETA = 0.5 + math.sqrt(3.0) / 6.0
+# (padded input width, padded output width) per layer; 8 inputs, 2 outputs
+LAYERS = [(16, 256), (256, 256), (256, 256), (256, 256), (256, 128)]
+N_IN, N_OUT = 8, 2
+
+
+def _p(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else ctypes.c_void_p(0)
+
+
+def _st():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def gemm(A, lda, sA, B, ldb, sB, M, N, K, P, bias=None, sBias=0, aux=None, ldaux=0, sAux=0,
+         out_f32=None, ldo=0, sO=0, out_bf16=None, ldh=0, sH=0, act=0, status=None):
+    g = _lib.Gemm(A.data_ptr(), lda, sA, B.data_ptr(), ldb, sB,
+                  bias.data_ptr() if bias is not None else None, sBias,
+                  aux.data_ptr() if aux is not None else None, ldaux, sAux,
+                  out_f32.data_ptr() if out_f32 is not None else None, ldo, sO,
+                  out_bf16.data_ptr() if out_bf16 is not None else None, ldh, sH,
+                  M, N, K, act, P, 0, status.data_ptr() if status is not None else None)
+    _lib.call("fdadi_mlp_gemm", ctypes.byref(g), _st())
+
+
+def transpose(x, rows, cols, P, out, stride_in=None):
+    _lib.call("fdadi_transpose_bf16", _p(x), cols, rows * cols if stride_in is None else stride_in,
+              _p(out), rows, rows * cols, rows, cols, P, _st())
+    return out
+
+
+class MLPEnsemble(object):
+    """P independent MLPs trained together on the same batches."""
+
+    def __init__(self, members=4, seed=0, device=None):
+        self.P = members
+        self.dev = device or torch.device("cuda", torch.cuda.current_device())
+        g = torch.Generator(device="cpu").manual_seed(seed)
+        self.W, self.b, self.Wb, self.WTb = [], [], [], []
+        self.mW, self.vW, self.mb, self.vb = [], [], [], []
+        for li, (K, N) in enumerate(LAYERS):
+            k_valid = N_IN if li == 0 else K
+            n_valid = N_OUT if li == len(LAYERS) - 1 else N
+            W = torch.zeros(self.P, N, K)
+            gain = math.sqrt(2.0) if li < len(LAYERS) - 1 else 0.5
+            a = gain * math.sqrt(3.0 / k_valid)
+            W[:, :n_valid, :k_valid] = (torch.rand(self.P, n_valid, k_valid, generator=g) * 2 - 1) * a
+            self.W.append(W.to(self.dev))
+            self.b.append(torch.zeros(self.P, N, device=self.dev))
+            self.Wb.append(self.W[-1].to(torch.bfloat16))
+            self.WTb.append(self.W[-1].transpose(1, 2).contiguous().to(torch.bfloat16))
+            for lst in (self.mW, self.vW):
+                lst.append(torch.zeros_like(self.W[-1]))
+            for lst in (self.mb, self.vb):
+                lst.append(torch.zeros_like(self.b[-1]))
+        self.step = 0
+        self.status = torch.zeros(1, dtype=torch.int32, device=self.dev)
+        self._bufs = {}
+        self.scales = (1.0, 1.0)
+        self.loss_weights = torch.tensor([1.0, 0.1], dtype=torch.float32, device=self.dev)
+
+    # -- buffers --
+    def bufs(self, M):
+        if M not in self._bufs:
+            P, d = self.P, self.dev
+            b = {"Y": [torch.empty(P, M, N, dtype=torch.float32, device=d) for _, N in LAYERS],
+                 "H": [torch.empty(P, M, N, dtype=torch.bfloat16, device=d) for _, N in LAYERS[:-1]],
+                 "dY": [torch.empty(P, M, N, dtype=torch.bfloat16, device=d) for _, N in LAYERS],
+                 "dYT": torch.empty(P, 256, M, dtype=torch.bfloat16, device=d),
+                 "XT": torch.empty(P, 256, M, dtype=torch.bfloat16, device=d),
+                 "X0T": torch.empty(16, M, dtype=torch.bfloat16, device=d),
+                 "dW": [torch.empty(P, N, K, dtype=torch.float32, device=d) for K, N in LAYERS],
+                 "db": [torch.empty(P, N, dtype=torch.float32, device=d) for _, N in LAYERS],
+                 "loss": torch.zeros(P, dtype=torch.float64, device=d)}
+            self._bufs[M] = b
+        return self._bufs[M]
+
+    # -- forward --
+    def forward(self, X, M):
+        """X: bf16 [M][16] (shared by the members). Returns fp32 [P][M][128]
+        whose first two columns are the scaled residual outputs."""
+        b = self.bufs(M)
+        P = self.P
+        A, lda, sA = X, 16, 0
+        for li, (K, N) in enumerate(LAYERS):
+            last = li == len(LAYERS) - 1
+            gemm(A, lda, sA, self.Wb[li], K, N * K, M, N, K, P, bias=self.b[li], sBias=N,
+                 out_f32=b["Y"][li], ldo=N, sO=M * N,
+                 out_bf16=None if last else b["H"][li], ldh=N, sH=M * N,
+                 act=0 if last else 1, status=self.status)
+            if not last:
+                A, lda, sA = b["H"][li], N, M * N
+        return b["Y"][-1]
+
+    # -- one training step --
+    def train_step(self, X, target, M, lr):
+        """X bf16 [M][16], target fp32 [M][2]."""
+        b = self.bufs(M)
+        P = self.P
+        Y5 = self.forward(X, M)
+        b["loss"].zero_()
+        _lib.call("fdadi_mlp_mse", _p(Y5), 128, M * 128, _p(target), _p(self.loss_weights),
+                  N_OUT, _p(b["dY"][-1]), 128, M * 128, M, 128, P, _p(b["loss"]), _st())
+        transpose(X, M, 16, 1, b["X0T"])
+        for li in range(len(LAYERS) - 1, -1, -1):
+            K, N = LAYERS[li]
+            dY = b["dY"][li]
+            # weight gradient dW = dY^T X_prev: [N][M] x [K][M]^T
+            transpose(dY, M, N, P, b["dYT"])
+            if li == 0:
+                XT, sXT = b["X0T"], 0
+            else:
+                transpose(b["H"][li - 1], M, K, P, b["XT"])
+                XT, sXT = b["XT"], K * M
+            gemm(b["dYT"], M, N * M, XT, M, sXT, N, K, M, P, out_f32=b["dW"][li], ldo=K,
+                 sO=N * K, status=self.status)
+            _lib.call("fdadi_mlp_colsum", _p(dY), N, M * N, _p(b["db"][li]), N, M, N, P, _st())
+            if li > 0:
+                # back-propagate through W and the previous SiLU: dY_prev = (dY W) * SiLU'(Y_prev)
+                gemm(dY, N, M * N, self.WTb[li], N, K * N, M, K, N, P, aux=b["Y"][li - 1], ldaux=K,
+                     sAux=M * K, out_bf16=b["dY"][li - 1], ldh=K, sH=M * K, act=2,
+                     status=self.status)
+        self.step += 1
+        for li, (K, N) in enumerate(LAYERS):
+            for p in range(P):
+                _lib.call("fdadi_mlp_adam", _p(self.W[li][p]), _p(b["dW"][li][p]),
+                          _p(self.mW[li][p]), _p(self.vW[li][p]), N * K, N, K, float(lr), 0.9,
+                          0.999, 1e-8, self.step, _p(self.Wb[li][p]), _p(self.WTb[li][p]), _st())
+            _lib.call("fdadi_mlp_adam", _p(self.b[li]), _p(b["db"][li]), _p(self.mb[li]),
+                      _p(self.vb[li]), P * N, 0, 0, float(lr), 0.9, 0.999, 1e-8, self.step, None,
+                      None, _st())
+        return b["loss"]
+
+    def check(self):
+        if int(self.status.item()) != 0:
+            raise RuntimeError("a tensor-core GEMM timed out waiting for its MMAs")
+
+
+class Featurizer(object):
+    """Queries [M][9] (S0, K, T, r, kappa, theta, sigma, rho, v0) -> network
+    inputs, control variate and in-box flags, on the device."""
+
+    def __init__(self, device):
+        self.dev = device
+        self.lo = torch.as_tensor(BOX_LO, device=device)
+        self.hi = torch.as_tensor(BOX_HI, device=device)
+
+    def __call__(self, Q):
+        M = Q.shape[0]
+        X = torch.empty(M, 16, dtype=torch.bfloat16, device=self.dev)
+        base = torch.empty(M, 2, dtype=torch.float64, device=self.dev)
+        inbox = torch.empty(M, dtype=torch.int32, device=self.dev)
+        _lib.call("fdadi_mlp_featurize", _p(Q), M, _p(self.lo), _p(self.hi), _p(X), _p(base),
+                  _p(inbox), _st())
+        return X, base, inbox
+
+
+def adi_price(queries, nS=256, nv=128, nt=200, chunk=4096, graph=False, spot_max_factor=8.0,
+              var_max=5.0, pool=None):
+    """FP64 ADI prices and deltas (HV theta = 1/2 + sqrt(3)/6 after two
+    implicit half-steps) for queries [n][9] on nS x nv grids; delta is the
+    centred non-uniform first derivative in S at the spot grid point."""
+    from .batch import HestonBatch
+    q = np.asarray(queries, dtype=np.float64)
+    n = q.shape[0]
+    price = np.empty(n)
+    delta = np.empty(n)
+    jobs = [(q[k, 0], q[k, 1], q[k, 8], nS, nv, spot_max_factor * q[k, 1], var_max)
+            for k in range(n)]
+    meshes = pool.map(_mesh_job, jobs, chunksize=64) if pool is not None else [_mesh_job(j) for j in jobs]
+    for c0 in range(0, n, chunk):
+        sl = slice(c0, min(n, c0 + chunk))
+        qs = q[sl]
+        ms = meshes[sl]
+        params = [(r[3], r[4], r[5], r[6], r[7]) for r in qs]
+        dts = qs[:, 2] / nt
+        b = HestonBatch(params, ms, scheme="hv", n_steps=nt - 1, dt=dts, theta=HV_THETA,
+                        implicit_steps=2, implicit_dt_factor=0.5, graph=graph)
+        V = b.pack([np.maximum(m[0][:, None] - r[1], 0.0) * np.ones((1, m[1].size))
+                    for m, r in zip(ms, qs)])
+        b.run(V)
+        idx = b.flat_index([(r[0], r[8]) for r in qs])
+        vals = [b.gather(V, idx + off).cpu().numpy() for off in (-nv, 0, nv)]
+        i_s = [(int(ix) - int(b.p_off[k])) // nv for k, ix in enumerate(idx.cpu().numpy())]
+        for k in range(len(qs)):
+            S = ms[k][0]
+            i = i_s[k]
+            di, dn = S[i] - S[i - 1], S[i + 1] - S[i]
+            s = di + dn
+            w = (-dn / (di * s), (-di + dn) / (di * dn), di / (dn * s))
+            price[c0 + k] = vals[1][k]
+            delta[c0 + k] = w[0] * vals[0][k] + w[1] * vals[1][k] + w[2] * vals[2][k]
+        del b, V
+    return price, delta
+
+
+def _mesh_job(a):
+    S0, K, v0, nS, nv, smax, vmax = a
+    return _mesh.heston_meshes(S0, K, v0, int(nS), int(nv), smax, vmax)
+
+
+def sobol_queries(n, seed=0, S0=100.0, lo=BOX_LO, hi=BOX_HI):
+    """n scrambled-Sobol draws in the box, as queries [n][9]."""
+    from scipy.stats import qmc
+    u = qmc.Sobol(d=8, scramble=True, seed=seed).random(n)
+    f = lo + u * (hi - lo)
+    q = np.empty((n, 9))
+    q[:, 0] = S0
+    q[:, 1] = S0 / f[:, 0]
+    q[:, 2:] = f[:, 1:]
+    return q
+
+
+class Surrogate(object):
+    """Trained ensemble + control variate + fallback gate."""
+
+    def __init__(self, members=4, seed=0, device=None, tol=5e-4):
+        self.dev = device or torch.device("cuda", torch.cuda.current_device())
+        self.net = MLPEnsemble(members, seed, self.dev)
+        self.feat = Featurizer(self.dev)
+        self.tol = tol
+
+    def targets(self, Q, price, delta):
+        """Scaled residual targets over the control variate (fp32 [n][2])."""
+        Qd = torch.as_tensor(Q, device=self.dev)
+        _, base, _ = self.feat(Qd)
+        base = base.cpu().numpy()
+        r0 = price / Q[:, 1] - base[:, 0]
+        r1 = delta - base[:, 1]
+        if not hasattr(self, "s"):
+            self.s = (1.0 / max(np.std(r0), 1e-12), 1.0 / max(np.std(r1), 1e-12))
+            self.net.scales = self.s
+        t = np.stack([r0 * self.s[0], r1 * self.s[1]], axis=1).astype(np.float32)
+        return t
+
+    def fit(self, Q, price, delta, epochs=50, batch=8192, lr=1e-3, seed=0, log=None):
+        T = torch.as_tensor(self.targets(Q, price, delta), device=self.dev)
+        X, _, _ = self.feat(torch.as_tensor(Q, device=self.dev))
+        n = Q.shape[0]
+        steps_per_epoch = max(1, n // batch)
+        total = epochs * steps_per_epoch
+        g = torch.Generator(device="cpu").manual_seed(seed)
+        step = 0
+        losses = []
+        for ep in range(epochs):
+            perm = torch.randperm(n, generator=g).to(self.dev)
+            ep_loss = 0.0
+            for s in range(steps_per_epoch):
+                idx = perm[s * batch:(s + 1) * batch]
+                lr_t = 0.5 * lr * (1 + math.cos(math.pi * step / total))
+                loss = self.net.train_step(X[idx].contiguous(), T[idx].contiguous(), batch, lr_t)
+                ep_loss += float(loss.mean().item()) if s == steps_per_epoch - 1 else 0.0
+                step += 1
+            losses.append(ep_loss)
+            if log:
+                log(ep, ep_loss)
+        self.net.check()
+        return losses
+
+    def predict(self, Q):
+        """Q: [n][9] device float64. Returns (price, delta, spread, fallback
+        flags, fallback count) on the device."""
+        M0 = Q.shape[0]
+        M = ((M0 + 127) // 128) * 128
+        if M != M0:
+            Q = torch.cat([Q, Q[-1:].expand(M - M0, 9)], 0)
+        X, base, inbox = self.feat(Q)
+        Y = self.net.forward(X, M)
+        d = self.dev
+        price = torch.empty(M, dtype=torch.float64, device=d)
+        delta = torch.empty(M, dtype=torch.float64, device=d)
+        spread = torch.empty(M, dtype=torch.float64, device=d)
+        fb = torch.empty(M, dtype=torch.int32, device=d)
+        cnt = torch.zeros(1, dtype=torch.int32, device=d)
+        _lib.call("fdadi_mlp_combine", _p(Y), 128, M * 128, self.net.P, M, _p(Q), _p(base),
+                  _p(inbox), float(self.s[0]), float(self.s[1]), float(self.tol), _p(price),
+                  _p(delta), _p(spread), _p(fb), _p(cnt), _st())
+        return price[:M0], delta[:M0], spread[:M0], fb[:M0], cnt
+
+    def price(self, Q_host, nS=256, nv=128, nt=200, pool=None):
+        """Surrogate prices with FP64 ADI fallback for flagged queries."""
+        Q = torch.as_tensor(np.asarray(Q_host, dtype=np.float64), device=self.dev)
+        p, dlt, spread, fb, cnt = self.predict(Q)
+        p, dlt, fbh = p.cpu().numpy(), dlt.cpu().numpy(), fb.cpu().numpy().astype(bool)
+        if fbh.any():
+            pa, da = adi_price(np.asarray(Q_host)[fbh], nS, nv, nt, pool=pool)
+            p[fbh], dlt[fbh] = pa, da
+        return p, dlt, fbh

@@ -278,6 +278,23 @@ int fdadi_mlp_adam(float *p, const float *g, float *m1, float *m2, int64_t n, in
                    int32_t cols, float lr, float b1, float b2, float eps, int32_t step, void *w,
                    void *wt, void *stream);
 
+/* Surrogate front end: queries [M][9] = (S0, K, T, r, kappa, theta, sigma,
+ * rho, v0) -> bf16 network inputs X [M][16] (features S0/K, T, r, kappa,
+ * theta, sigma, rho, v0 mapped to [-1, 1] by the box lo/hi [8]), the
+ * Black-Scholes control variate base [M][2] = (price/K, delta) at the
+ * expected mean variance, and inbox [M]. */
+int fdadi_mlp_featurize(const double *queries, int32_t M, const double *lo, const double *hi,
+                        void *X, double *base, int32_t *inbox, void *stream);
+
+/* Ensemble read-out: y [problems][M][ldy] scaled residual outputs ->
+ * price = K (base0 + mean y0 / s0), delta = base1 + mean y1 / s1, spread =
+ * max - min of the members' prices, fallback = out of box or spread > tol*K;
+ * *count += number of fallbacks. */
+int fdadi_mlp_combine(const float *y, int64_t ldy, int64_t stride, int32_t problems, int32_t M,
+                      const double *queries, const double *base, const int32_t *inbox, double s0,
+                      double s1, double tol, double *price, double *delta, double *spread,
+                      int32_t *fallback, int32_t *count, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,121 @@
+"""Surrogate: tensor-core training gradients against a float64 CPU oracle,
+and a small end-to-end run on ADI-priced options."""
+import time
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def dev():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from fd_adi_gb300 import _lib
+    _lib.load()
+    return torch.device("cuda", 0)
+
+
+def _bf(x):
+    return x.to(torch.bfloat16).to(torch.float64)
+
+
+def _cpu_grads(net, X, T, M, mimic_rounding):
+    """float64 CPU forward/backward of the same network; with mimic_rounding
+    the bf16 rounding points of the device pipeline are reproduced."""
+    from fd_adi_gb300.surrogate import LAYERS
+    P = net.P
+    r = _bf if mimic_rounding else (lambda x: x)
+    W = [net.Wb[l].cpu().to(torch.float64) for l in range(len(LAYERS))]
+    b = [net.b[l].cpu().to(torch.float64) for l in range(len(LAYERS))]
+    w = net.loss_weights.cpu().to(torch.float64)
+    X = X.cpu().to(torch.float64)
+    T = T.cpu().to(torch.float64)
+    gW, gb = [], []
+    for p in range(P):
+        Hs, Ys = [X], []
+        H = X
+        for l in range(len(LAYERS)):
+            Y = H @ W[l][p].T + b[l][p]
+            Ys.append(Y)
+            if l < len(LAYERS) - 1:
+                H = r(torch.nn.functional.silu(Y))
+                Hs.append(H)
+        dY = torch.zeros_like(Ys[-1])
+        dY[:, :2] = 2 * w * (Ys[-1][:, :2] - T) / M
+        dY = r(dY)
+        gWp, gbp = [None] * len(LAYERS), [None] * len(LAYERS)
+        for l in range(len(LAYERS) - 1, -1, -1):
+            gWp[l] = dY.T @ Hs[l]
+            gbp[l] = dY.sum(0)
+            if l > 0:
+                s = torch.sigmoid(Ys[l - 1])
+                dY = r((dY @ W[l][p]) * (s * (1 + Ys[l - 1] * (1 - s))))
+        gW.append(gWp)
+        gb.append(gbp)
+    return gW, gb
+
+
+def test_training_gradients_match_cpu_oracle(dev):
+    from fd_adi_gb300.surrogate import MLPEnsemble, LAYERS
+    M = 256
+    net = MLPEnsemble(members=2, seed=3, device=dev)
+    g = torch.Generator(device="cpu").manual_seed(1)
+    X = torch.zeros(M, 16)
+    X[:, :8] = torch.rand(M, 8, generator=g) * 2 - 1
+    X = X.to(torch.bfloat16).to(dev)
+    T = (torch.randn(M, 2, generator=g)).to(dev)
+    net.train_step(X, T, M, lr=0.0)
+    net.check()
+    bufs = net.bufs(M)
+    for mimic, tol in ((True, 2e-3), (False, 5e-2)):
+        gW, gb = _cpu_grads(net, X, T, M, mimic)
+        for p in range(net.P):
+            for l in range(len(LAYERS)):
+                got = bufs["dW"][l][p].cpu().to(torch.float64)
+                ref = gW[p][l]
+                scale = ref.abs().max().item()
+                assert (got - ref).abs().max().item() <= tol * scale, (mimic, p, l)
+                gotb = bufs["db"][l][p].cpu().to(torch.float64)
+                assert (gotb - gb[p][l]).abs().max().item() <= tol * gb[p][l].abs().max().item() + 1e-12
+
+
+def test_surrogate_learns_adi_prices_and_gates(dev):
+    from fd_adi_gb300.surrogate import Surrogate, adi_price, sobol_queries
+    grid = dict(nS=64, nv=32, nt=40)
+    Qtr = sobol_queries(4096, seed=1)
+    Qte = sobol_queries(512, seed=2)
+    t0 = time.perf_counter()
+    ptr, dtr = adi_price(Qtr, **grid)
+    torch.cuda.synchronize()
+    t_adi = (time.perf_counter() - t0) / Qtr.shape[0]
+    pte, dte = adi_price(Qte, **grid)
+    sur = Surrogate(members=4, seed=0, device=dev)
+    losses = sur.fit(Qtr, ptr, dtr, epochs=40, batch=512, lr=2e-3)
+    assert losses[-1] < 0.2 * losses[0]
+    Q = torch.as_tensor(Qte, device=dev)
+    p, d, spread, fb, cnt = sur.predict(Q)
+    p = p.cpu().numpy()
+    # the control variate alone (the features' Black-Scholes price)
+    _, base, _ = sur.feat(Q)
+    p_cv = base[:, 0].cpu().numpy() * Qte[:, 1]
+    err_net = np.sqrt(np.mean((p - pte) ** 2))
+    err_cv = np.sqrt(np.mean((p_cv - pte) ** 2))
+    assert err_net < 0.5 * err_cv, (err_net, err_cv)
+    # queries outside the box always fall back to ADI
+    Qout = Qte[:128].copy()
+    Qout[:, 2] = 4.0                       # T beyond the box
+    _, _, _, fbo, _ = sur.predict(torch.as_tensor(Qout, device=dev))
+    assert bool(fbo.bool().all())
+    # inference is much cheaper than pricing by ADI
+    Qbig = torch.as_tensor(np.tile(Qte, (64, 1)), device=dev)
+    sur.predict(Qbig)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sur.predict(Qbig)
+    torch.cuda.synchronize()
+    t_sur = (time.perf_counter() - t0) / Qbig.shape[0]
+    assert t_sur * 100 < t_adi
