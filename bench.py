@@ -297,6 +297,111 @@ def plain_vs_batched(torch, n_batch=2048):
             "price_rel_diff": abs(p_plain - p_batch) / abs(p_plain)}
 
 
+def run_surrogate(args):
+    """Learned surrogate with ADI fallback (the surrogate configurations):
+    training set of scrambled-Sobol draws in the batched box priced by the
+    batched FP64 ADI at 256x128x200; a 4-member BF16 ensemble trained on the
+    tensor cores (lr 1e-3 cosine, batch 8192); queries 95% inside the box and
+    5% outside (T up to 5, sigma up to 2) priced by surrogate + fallback."""
+    import multiprocessing as mp
+    import torch
+    from fd_adi_gb300 import _lib
+    from fd_adi_gb300.surrogate import (Surrogate, adi_price, sobol_queries, BOX_LO, BOX_HI,
+                                        MLPEnsemble, LAYERS)
+    torch.cuda.set_device(0)
+    _lib.load()
+    dev = torch.device("cuda", 0)
+    grid = dict(nS=256, nv=128, nt=200)
+    pool = mp.get_context("spawn").Pool(min(16, os.cpu_count() or 1))
+    t0 = time.perf_counter()
+    Qtr = sobol_queries(args.train, seed=args.seed + 1)
+    Qte = sobol_queries(args.test, seed=args.seed + 2)
+    ptr, dtr = adi_price(Qtr, pool=pool, **grid)
+    pte, dte = adi_price(Qte, pool=pool, **grid)
+    torch.cuda.synchronize()
+    t_data = time.perf_counter() - t0
+    adi_rate = (args.train + args.test) / t_data
+    sur = Surrogate(members=4, seed=args.seed, device=dev)
+    t0 = time.perf_counter()
+    sur.fit(Qtr, ptr, dtr, epochs=args.epochs, batch=8192, lr=1e-3)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    p, d, spread, fb, _ = sur.predict(torch.as_tensor(Qte, device=dev))
+    p = p.cpu().numpy()
+    d = d.cpu().numpy()
+    err = np.abs(p - pte)
+    # queries: 95% in the box, 5% outside it
+    rng = np.random.default_rng(args.seed + 3)
+    nq = args.queries
+    Q = sobol_queries(nq, seed=args.seed + 4)
+    out = rng.random(nq) < 0.05
+    Q[out, 2] = rng.uniform(0.1, 5.0, out.sum())
+    Q[out, 6] = rng.uniform(0.1, 2.0, out.sum())
+    def step():
+        return sur.price(Q, pool=pool, **grid)
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        pq, dq, fbq = step()
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    value = nq / float(np.mean(times))
+    # accuracy of the served prices on a sample, against FP64 ADI
+    ns = min(args.sample, nq)
+    sidx = np.linspace(0, nq - 1, ns).astype(int)
+    pref, _ = adi_price(Q[sidx], pool=pool, **grid)
+    qerr = np.abs(pq[sidx] - pref)
+    # tensor pipe: one ensemble forward on the query batch, timed with events
+    Qd = torch.as_tensor(Q, device=dev)
+    M = (nq // 128) * 128
+    X, _, _ = sur.feat(Qd[:M].contiguous())
+    sur.net.forward(X, M)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(5):
+        sur.net.forward(X, M)
+    e1.record()
+    torch.cuda.synchronize()
+    fwd_ms = e0.elapsed_time(e1) / 5
+    flops = 2.0 * M * sur.net.P * sum(k * n for k, n in LAYERS)
+    with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+        peak = float(json.load(f).get("bf16_tflops", 1901.1))
+    ach = flops / (fwd_ms * 1e-3) / 1e12
+    pool.close()
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": float(np.mean(times)) * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16 network (fp32 accumulate) + f64 ADI fallback", "data": "synthetic",
+            "config": {"workload": "surrogate + ADI fallback: %d queries (95%% in box, 5%% "
+                                   "outside: T<=5, sigma<=2); 4-member BF16 MLP 8-256x4-2 "
+                                   "trained on %d Sobol draws priced by FP64 ADI 256x128x200"
+                                   % (nq, args.train),
+                       "train": args.train, "test": args.test, "epochs": args.epochs,
+                       "batch": 8192, "grid": "256x128x200 HV + Rannacher",
+                       "parallelism": "dp1"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": int(Q.nbytes),
+                    "d2h_bytes_per_step": int(nq * 8 * 3)},
+            "roofline": {"bound": "tensor", "kernel": "umma_gemm (ensemble forward)",
+                         "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
+                         "traffic": None, "peak_source": "measured (MEASURED_PEAKS.json burst)"},
+            "surrogate": {"heldout_max_abs_err": float(err.max()),
+                          "heldout_rms_abs_err": float(np.sqrt(np.mean(err ** 2))),
+                          "heldout_delta_rms_err": float(np.sqrt(np.mean((d - dte) ** 2))),
+                          "heldout_fallback_fraction": float(fb.float().mean().item()),
+                          "query_fallback_fraction": float(fbq.mean()),
+                          "query_max_abs_err": float(qerr.max()),
+                          "query_rms_abs_err": float(np.sqrt(np.mean(qerr ** 2))),
+                          "batched_adi_options_per_s": adi_rate,
+                          "speedup_vs_batched_adi": value / adi_rate,
+                          "data_gen_s": t_data, "train_s": t_train,
+                          "forward_ms": fwd_ms}}
+    print(json.dumps(line))
+    return 0
+
+
 def cpu_baseline(w, n_sample, nt_sample=None):
     """The oracle (C restatement of the reference engine, one OpenMP thread
     per option) on this host's cores, on n_sample options spread through the
@@ -380,7 +485,12 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=32)
     ap.add_argument("--cpu-sample", type=int, default=32)
     ap.add_argument("--no-extras", action="store_true")
-    ap.add_argument("--workload", default="batch", choices=["batch", "config2"])
+    ap.add_argument("--workload", default="batch", choices=["batch", "config2", "surrogate"])
+    ap.add_argument("--train", type=int, default=1 << 17)
+    ap.add_argument("--test", type=int, default=1 << 13)
+    ap.add_argument("--queries", type=int, default=100000)
+    ap.add_argument("--epochs", type=int, default=50)
+    ap.add_argument("--sample", type=int, default=2000)
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -389,6 +499,8 @@ def main():
 
     if args.impl == "reference":
         return run_reference(args, rank, world)
+    if args.workload == "surrogate":
+        return run_surrogate(args) if rank == 0 else 0
 
     import torch
     import torch.distributed as dist
