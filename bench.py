@@ -297,6 +297,41 @@ def plain_vs_batched(torch, n_batch=2048):
             "price_rel_diff": abs(p_plain - p_batch) / abs(p_plain)}
 
 
+def run_gemm(args):
+    """Ensemble forward of the surrogate network alone on --queries random
+    inputs (4 members, 8-256x4-2): tensor-core GEMM throughput."""
+    import torch
+    from fd_adi_gb300 import _lib
+    from fd_adi_gb300.surrogate import MLPEnsemble, LAYERS
+    torch.cuda.set_device(0)
+    _lib.load()
+    dev = torch.device("cuda", 0)
+    M = (args.queries // 128) * 128
+    net = MLPEnsemble(members=4, seed=args.seed, device=dev)
+    X = torch.zeros(M, 16)
+    X[:, :8] = torch.rand(M, 8) * 2 - 1
+    X = X.to(torch.bfloat16).to(dev)
+    for _ in range(args.warmup):
+        net.forward(X, M)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        net.forward(X, M)
+    e1.record()
+    torch.cuda.synchronize()
+    net.check()
+    ms = e0.elapsed_time(e1) / args.steps
+    flops = 2.0 * M * net.P * sum(k * n for k, n in LAYERS)
+    with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+        peak = float(json.load(f).get("bf16_tflops", 1901.1))
+    ach = flops / (ms * 1e-3) / 1e12
+    print(json.dumps({"workload": "surrogate ensemble forward", "queries": M, "ms": ms,
+                      "queries_per_s": M / (ms * 1e-3), "tflops": ach, "peak": peak,
+                      "frac": ach / peak}))
+    return 0
+
+
 def run_surrogate(args):
     """Learned surrogate with ADI fallback (the surrogate configurations):
     training set of scrambled-Sobol draws in the batched box priced by the
@@ -403,33 +438,53 @@ def run_surrogate(args):
 
 
 def cpu_baseline(w, n_sample, nt_sample=None):
-    """The oracle (C restatement of the reference engine, one OpenMP thread
-    per option) on this host's cores, on n_sample options spread through the
-    workload and, when nt_sample is given, only that many HV steps of each."""
-    from oracle import oracle as O
+    """The reference CPU engine (compiled from its generated sources on this
+    host, kind "reference") or, where it does not import, the C restatement
+    of it (kind "port"), on all host cores (one single-threaded process per
+    core, options spread over them), on n_sample options spread through the
+    workload and, when nt_sample is given, only that many time steps of each.
+    The sample's grid-point-step rate is converted to options of the
+    workload's mean grid size."""
     n = len(w["K"])
     idx = sorted(set(np.linspace(0, n - 1, n_sample).astype(int).tolist()))
-    meshes = meshes_for(w, idx)
-    V0 = payoffs(w, meshes, idx)
     nt = w["nt"]
     nrun = nt if nt_sample is None else nt_sample
-    scheds = [[("implicit", 2, w["T"][k] / nt / 2, 1.0), ("hv", nrun - 1, w["T"][k] / nt, HV_THETA)]
-              for k in idx]
     cores = os.cpu_count() or 1
-    O.build()
-    t0 = time.perf_counter()
-    O.heston_batch(meshes, params_of(w, idx), V0, scheds, nthreads=cores)
-    dt = time.perf_counter() - t0
-    pts = float(sum(int(w["nS"][k]) * int(w["nv"][k]) for k in idx)) * nrun
-    # the sample's grid-point-step rate, converted to options of the full
-    # workload's mean grid size
     mean_pts = float(np.mean(w["nS"].astype(np.int64) * w["nv"])) * nt
-    return {"value": pts / dt / mean_pts, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": "%d options spread through the %d-option workload, %d of %d time steps "
-                      "(%.3g grid-point-steps), %d cores, %.1f s: %.3g grid-point-steps/s, "
-                      "scaled to the workload's mean option" % (len(idx), n, nrun, nt, pts,
-                                                                 min(cores, len(idx)), dt,
-                                                                 pts / dt)}
+    from oracle import ref_harness as H
+    if H.available():
+        import multiprocessing as mp
+        for var in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
+            os.environ[var] = "1"
+        jobs = [(w["S0"], w["K"][k], w["r"][k], w["kappa"][k], w["theta"][k], w["sigma"][k],
+                 w["rho"][k], w["v0"][k], w["T"][k] * nrun / nt, w["nS"][k], w["nv"][k], nrun)
+                for k in idx]
+        with mp.get_context("spawn").Pool(min(cores, len(jobs))) as pool:
+            pool.map(H.price_option, jobs[:1])       # warm the workers' imports
+            t0 = time.perf_counter()
+            res = pool.map(H.price_option, jobs, chunksize=1)
+            dt = time.perf_counter() - t0
+        kind = "reference"
+        what = "reference CPU engine (FiniteDifferenceEngine.pyx, compat build)"
+    else:
+        from oracle import oracle as O
+        meshes = meshes_for(w, idx)
+        V0 = payoffs(w, meshes, idx)
+        scheds = [[("implicit", 2, w["T"][k] / nt / 2, 1.0),
+                   ("hv", nrun - 1, w["T"][k] / nt, HV_THETA)] for k in idx]
+        O.build()
+        t0 = time.perf_counter()
+        O.heston_batch(meshes, params_of(w, idx), V0, scheds, nthreads=cores)
+        dt = time.perf_counter() - t0
+        kind = "port"
+        what = "C restatement of the reference engine (oracle)"
+    pts = float(sum(int(w["nS"][k]) * int(w["nv"][k]) for k in idx)) * nrun
+    return {"value": pts / dt / mean_pts, "unit": UNIT, "cores": min(cores, len(idx)),
+            "kind": kind,
+            "sample": "%s: %d options spread through the %d-option workload, %d of %d time "
+                      "steps (%.3g grid-point-steps) on %d cores in %.1f s = %.3g "
+                      "grid-point-steps/s, scaled to the workload's mean option"
+                      % (what, len(idx), n, nrun, nt, pts, min(cores, len(idx)), dt, pts / dt)}
 
 
 def run_reference(args, rank, world):
@@ -485,7 +540,7 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=32)
     ap.add_argument("--cpu-sample", type=int, default=32)
     ap.add_argument("--no-extras", action="store_true")
-    ap.add_argument("--workload", default="batch", choices=["batch", "config2", "surrogate"])
+    ap.add_argument("--workload", default="batch", choices=["batch", "config2", "surrogate", "gemm"])
     ap.add_argument("--train", type=int, default=1 << 17)
     ap.add_argument("--test", type=int, default=1 << 13)
     ap.add_argument("--queries", type=int, default=100000)
@@ -501,6 +556,8 @@ def main():
         return run_reference(args, rank, world)
     if args.workload == "surrogate":
         return run_surrogate(args) if rank == 0 else 0
+    if args.workload == "gemm":
+        return run_gemm(args) if rank == 0 else 0
 
     import torch
     import torch.distributed as dist

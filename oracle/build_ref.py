@@ -27,6 +27,11 @@ Compat edits (all made on the copies, never on the reference tree):
 
 Usage: ``python oracle/build_ref.py`` (needs Cython, run in a container where
 the reference tree exists). Exits 0 and prints ``skipped`` if it does not.
+
+``python oracle/build_ref.py --from-generated`` compiles the C/C++ files that
+an earlier run generated (already under ``oracle/_ref/``) with this machine's
+compiler, Python and numpy headers, without Cython or the reference tree: the
+GPU host uses this to run the reference engine as the CPU baseline.
 """
 import os
 import re
@@ -80,7 +85,38 @@ def _edit(path, subs):
         f.write(s)
 
 
+def build_generated():
+    """Compile the generated BandedOperator.cpp, FiniteDifferenceEngine.cpp,
+    utils.c and Option.c in place (no Cython needed)."""
+    import sysconfig
+    srcs = {"BandedOperator": "BandedOperator.cpp",
+            "FiniteDifferenceEngine": "FiniteDifferenceEngine.cpp",
+            "utils": "utils.c", "Option": "Option.c"}
+    if not all(os.path.exists(os.path.join(PKG, f)) for f in srcs.values()):
+        print("build_ref: no generated sources, skipped")
+        return 0
+    suffix = sysconfig.get_config_var("EXT_SUFFIX")
+    if all(os.path.exists(os.path.join(PKG, m + suffix)) for m in srcs):
+        print("build_ref: already built")
+        return 0
+    import numpy
+    inc = [sysconfig.get_paths()["include"], numpy.get_include()]
+    procs = []
+    for mod, src in srcs.items():
+        cc = "g++" if src.endswith(".cpp") else "gcc"
+        cmd = [cc, "-O2", "-w", "-shared", "-fPIC"] + ["-I" + i for i in inc] + \
+              [os.path.join(PKG, src), "-o", os.path.join(PKG, mod + suffix)]
+        procs.append(subprocess.Popen(cmd))
+    rc = max(p.wait() for p in procs)
+    if rc:
+        raise RuntimeError("compiling the generated reference sources failed")
+    print("build_ref: built from generated sources", PKG)
+    return 0
+
+
 def main():
+    if "--from-generated" in sys.argv:
+        return build_generated()
     if not os.path.isdir(REF):
         print("build_ref: reference tree absent, skipped")
         return 0

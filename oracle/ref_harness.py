@@ -8,8 +8,10 @@ coefficient dict (heston.py:302-333), boundary dict (heston.py:335-359) and
 grid construction (heston.py:380-406) are restated here in Python 3 and handed
 to the reference ``FiniteDifferenceEngineADI`` unchanged.
 
-Only usable in a container where the reference tree was built; nothing in the
-product or in the GPU tests imports this module.
+Usable where the reference was compat-built from its sources
+(``oracle/build_ref.py``) or where its generated C/C++ was compiled
+(``oracle/build_ref.py --from-generated``, the GPU host). Only the tests and
+the CPU-baseline leg of ``bench.py`` import this module.
 """
 import contextlib
 import io
@@ -23,7 +25,14 @@ _REF = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_ref")
 
 
 def available():
-    return os.path.isdir(os.path.join(_REF, "FiniteDifference"))
+    """True if the compiled reference modules import on this machine."""
+    if not os.path.isdir(os.path.join(_REF, "FiniteDifference")):
+        return False
+    try:
+        _import()
+        return True
+    except ImportError:
+        return False
 
 
 def _import():
@@ -108,3 +117,23 @@ def price_index(spots, vars_, S0, v0):
 def quiet(fn, *a, **k):
     with contextlib.redirect_stdout(io.StringIO()):
         return fn(*a, **k)
+
+
+def price_option(job):
+    """Price one Heston call with the reference engine (for a process pool):
+    job = (S0, K, r, kappa, theta, sigma, rho, v0, T, nS, nv, nt); the mesh as
+    the reference builds it (S_max = 8K, v_max = 5), two implicit half-steps then
+    HV theta = 1/2 + sqrt(3)/6 for the remaining steps. Returns (price,
+    grid-point-steps, seconds of the time loop)."""
+    import time
+    S0, K, r, kappa, theta, sigma, rho, v0, T, nS, nv, nt = job
+    spots, vars_ = heston_mesh(S0, K, v0, int(nS), int(nv), 8.0 * K, 5.0)
+    F = heston_engine(S0, K, r, v0, kappa, theta, sigma, rho, spots, vars_)
+    V0 = F.grid.domain[-1].copy()
+    dt = T / nt
+    t0 = time.perf_counter()
+    V = quiet(F.solve_implicit, 2, dt * 0.5, initial=V0)
+    V = quiet(F.solve_hundsdorferverwer, int(nt) - 1, dt, initial=V,
+              theta=0.5 + np.sqrt(3.0) / 6.0)
+    t = time.perf_counter() - t0
+    return float(V[price_index(spots, vars_, S0, v0)]), float(nS) * nv * nt, t
