@@ -8,14 +8,16 @@
 // fused epilogue (bias, SiLU, multiplication by SiLU'(aux), fp32 and/or bf16
 // stores). Transposed operands are produced by a separate transpose kernel.
 //
-// A CTA (4 warps) owns one 128 x N tile. For each K chunk of 64 it stages the
-// A and B chunks in shared memory in the canonical no-swizzle K-major layout
-// (8-row x 16-byte core matrices: core matrices adjacent in K are 128 bytes
-// apart, 8-row groups are chunk/8 * 128 bytes apart), one elected thread
-// issues the tcgen05.mma instructions (K = 16 each) accumulating into tensor
-// memory and commits them to an mbarrier; every wait on that mbarrier is
-// bounded and sets the status word instead of hanging. The epilogue reads the
-// accumulator rows with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31).
+// A CTA (4 warps) owns one 128 x N tile. K chunks of 64 are copied with
+// cp.async (every 16-byte copy of a chunk in flight at once) into two
+// shared-memory stages in the canonical no-swizzle K-major layout (8-row x
+// 16-byte core matrices: core matrices adjacent in K are 128 bytes apart,
+// 8-row groups are chunk/8 * 128 bytes apart), so chunk k+1 loads while the
+// MMAs of chunk k run. One elected thread issues the tcgen05.mma instructions
+// (K = 16 each) accumulating into tensor memory and commits them to the
+// stage's mbarrier; every wait on an mbarrier is bounded and sets the status
+// word instead of hanging. The epilogue reads the accumulator rows with
+// tcgen05.ld (warp w owns TMEM lanes 32w..32w+31) and stores 16-byte vectors.
 #include <cuda_bf16.h>
 #include <stdint.h>
 
@@ -30,8 +32,9 @@ constexpr int GM_BK = 64;           // K chunk staged per MMA round
 constexpr int GM_THREADS = 128;
 constexpr int GM_A_BYTES = GM_BM * GM_BK * 2;      // 16 KB
 constexpr int GM_B_BYTES = 256 * GM_BK * 2;        // 32 KB (N <= 256)
-constexpr int GM_SMEM = 100 * 1024; // requested per CTA: two CTAs per SM, so two
-                                    // 256-column accumulators fit in TMEM (512)
+constexpr int GM_SMEM = 100 * 1024; // two stages of A and B (96 KB) + barriers; two
+                                    // CTAs per SM, so two 256-column accumulators fit
+                                    // in TMEM (512 columns)
 constexpr long long GM_WAIT_CYCLES = 4000000000LL;  // ~2 s at 2 GHz
 
 struct GemmArgs {
@@ -74,12 +77,31 @@ __device__ __forceinline__ float dsilu(float x) {
     return s * (1.0f + x * (1.0f - s));
 }
 
+__device__ __forceinline__ void cp_async16(uint32_t saddr, const void *g) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(saddr), "l"(g));
+}
+
+// Bounded wait on an mbarrier phase; false if it timed out.
+__device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity) {
+    const long long t0 = clock64();
+    uint32_t done = 0;
+    while (!done) {
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+            "selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done) : "r"(smem_addr(mbar)), "r"(parity));
+        if (!done && clock64() - t0 > GM_WAIT_CYCLES) return false;
+    }
+    return true;
+}
+
 __global__ void __launch_bounds__(GM_THREADS) umma_gemm_kernel(GemmArgs g) {
     extern __shared__ __align__(1024) unsigned char smem[];
-    unsigned char *sA = smem;
-    unsigned char *sB = smem + GM_A_BYTES;
-    uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + GM_A_BYTES + GM_B_BYTES);
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + GM_A_BYTES + GM_B_BYTES + 8);
+    // two stages of (A tile, B tile); K chunk k lives in stage k % 2
+    constexpr uint32_t STAGE = GM_A_BYTES + GM_B_BYTES;
+    const uint32_t sbase = smem_addr(smem);  // stage st: A at sbase + st * STAGE, B after it
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + 2 * (GM_A_BYTES + GM_B_BYTES));
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + 2 * (GM_A_BYTES + GM_B_BYTES) + 16);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int prob = blockIdx.y;
     const int m0 = blockIdx.x * GM_BM;
@@ -94,7 +116,8 @@ __global__ void __launch_bounds__(GM_THREADS) umma_gemm_kernel(GemmArgs g) {
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(mbar)));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&mbar[0])));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&mbar[1])));
         asm volatile("fence.mbarrier_init.release.cluster;");
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
@@ -103,61 +126,74 @@ __global__ void __launch_bounds__(GM_THREADS) umma_gemm_kernel(GemmArgs g) {
     const uint32_t tmem = *tslot;
     const uint32_t idesc = umma_idesc(GM_BM, N);
 
-    bool ok = true;
-    uint32_t phase = 0;
-    for (int k0 = 0; k0 < K; k0 += GM_BK) {
-        const int kw = min(GM_BK, K - k0);     // multiple of 16
-        const int kc = kw >> 3;                // 16-byte core-matrix columns
+    // 16-byte chunk (row r, column c) of a K chunk goes to
+    // (r / 8) * sbo + c * 128 + (r % 8) * 16, sbo = (chunk width / 8) * 128
+    auto issue = [&](int k0, int st) {
+        const int kw = min(GM_BK, K - k0), kc = kw >> 3;
         const uint32_t sbo = (uint32_t)kc * 128;
-        // stage A (128 rows) and B (N rows): 16-byte chunk (row r, column c)
-        // goes to (r / 8) * sbo + c * 128 + (r % 8) * 16
+        const uint32_t a0 = sbase + st * STAGE, b0 = a0 + GM_A_BYTES;
         for (int q = tid; q < GM_BM * kc; q += GM_THREADS) {
             const int r = q / kc, c = q - r * kc;
-            const uint4 v = *reinterpret_cast<const uint4 *>(A + (int64_t)(m0 + r) * g.lda + k0 + c * 8);
-            *reinterpret_cast<uint4 *>(sA + (r >> 3) * sbo + c * 128 + (r & 7) * 16) = v;
+            cp_async16(a0 + (r >> 3) * sbo + c * 128 + (r & 7) * 16,
+                       A + (int64_t)(m0 + r) * g.lda + k0 + c * 8);
         }
         for (int q = tid; q < N * kc; q += GM_THREADS) {
             const int r = q / kc, c = q - r * kc;
-            const uint4 v = *reinterpret_cast<const uint4 *>(B + (int64_t)r * g.ldb + k0 + c * 8);
-            *reinterpret_cast<uint4 *>(sB + (r >> 3) * sbo + c * 128 + (r & 7) * 16) = v;
+            cp_async16(b0 + (r >> 3) * sbo + c * 128 + (r & 7) * 16,
+                       B + (int64_t)r * g.ldb + k0 + c * 8);
         }
+        asm volatile("cp.async.commit_group;");
+    };
+
+    bool ok = true;
+    uint32_t phase = 0u;  // bit st = parity of stage st's next mbarrier phase
+    const int nk = (K + GM_BK - 1) / GM_BK;
+    issue(0, 0);
+    for (int kk = 0; kk < nk; ++kk) {
+        const int st = kk & 1, k0 = kk * GM_BK;
+        const int kw = min(GM_BK, K - k0);
+        const uint32_t sbo = (uint32_t)(kw >> 3) * 128;
+        asm volatile("cp.async.wait_group 0;");
         asm volatile("fence.proxy.async.shared::cta;");
         __syncthreads();
         if (tid == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;");
             for (int s = 0; s < (kw >> 4); ++s) {
-                const uint64_t ad = umma_desc(smem_addr(sA) + s * 256, 128, sbo);
-                const uint64_t bd = umma_desc(smem_addr(sB) + s * 256, 128, sbo);
-                const uint32_t acc = (k0 > 0 || s > 0) ? 1u : 0u;
+                const uint32_t a0 = sbase + st * STAGE;
+                const uint64_t ad = umma_desc(a0 + s * 256, 128, sbo);
+                const uint64_t bd = umma_desc(a0 + GM_A_BYTES + s * 256, 128, sbo);
+                const uint32_t acc = (kk > 0 || s > 0) ? 1u : 0u;
                 asm volatile(
                     "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
                     "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
                     ::"r"(tmem), "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
             }
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
-                         ::"r"(smem_addr(mbar)));
+                         ::"r"(smem_addr(&mbar[st])));
         }
-        // bounded wait for the MMAs of this chunk (they read sA/sB)
-        const long long t0 = clock64();
-        uint32_t done = 0;
-        while (!done) {
-            asm volatile(
-                "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-                "selp.u32 %0, 1, 0, p;\n}\n"
-                : "=r"(done) : "r"(smem_addr(mbar)), "r"(phase));
-            if (!done && clock64() - t0 > GM_WAIT_CYCLES) {
-                ok = false;
-                break;
+        if (kk + 1 < nk) {
+            const int ns = st ^ 1;
+            if (kk >= 1) {
+                // the MMAs of chunk kk - 1 read stage ns: wait before refilling it
+                const bool w = mbar_wait(&mbar[ns], (phase >> ns) & 1u);
+                phase ^= 1u << ns;
+                if (!__syncthreads_and(w ? 1 : 0)) {
+                    ok = false;
+                    break;
+                }
             }
-        }
-        phase ^= 1u;
-        // every thread reaches this barrier, timed out or not, so the
-        // decision to stop is the same for the whole block
-        if (!__syncthreads_and(ok ? 1 : 0)) {
-            ok = false;
-            break;
+            issue(k0 + GM_BK, ns);
         }
     }
+    if (ok) {
+        // the last commit covers every MMA issued before it; the one before it
+        // (other stage) is waited too, so no arrive reaches shared memory after exit
+        const int last = (nk - 1) & 1;
+        bool w = mbar_wait(&mbar[last], (phase >> last) & 1u);
+        if (nk >= 2) w = mbar_wait(&mbar[last ^ 1], (phase >> (last ^ 1)) & 1u) && w;
+        if (!__syncthreads_and(w ? 1 : 0)) ok = false;
+    }
+    asm volatile("cp.async.wait_group 0;");
     asm volatile("tcgen05.fence::after_thread_sync;");
     if (!ok) {
         if (tid == 0 && g.status) atomicExch(g.status, 1);
@@ -176,15 +212,27 @@ __global__ void __launch_bounds__(GM_THREADS) umma_gemm_kernel(GemmArgs g) {
                   "=r"(r[6]), "=r"(r[7])
                 : "r"(taddr));
             asm volatile("tcgen05.wait::ld.sync.aligned;");
+            float x[8];
 #pragma unroll
             for (int e = 0; e < 8; ++e) {
-                float x = __uint_as_float(r[e]);
-                const int n = c0 + e;
-                if (bias) x += bias[n];
-                if (of) of[n] = x;
-                if (g.act == 1) x = silu(x);
-                else if (g.act == 2) x *= dsilu(aux[n]);
-                if (oh) oh[n] = __float2bfloat16(x);
+                x[e] = __uint_as_float(r[e]);
+                if (bias) x[e] += bias[c0 + e];
+            }
+            if (of) {
+                float4 *o4 = reinterpret_cast<float4 *>(of + c0);
+                o4[0] = make_float4(x[0], x[1], x[2], x[3]);
+                o4[1] = make_float4(x[4], x[5], x[6], x[7]);
+            }
+            if (oh) {
+                __align__(16) bf16 h[8];
+#pragma unroll
+                for (int e = 0; e < 8; ++e) {
+                    float y = x[e];
+                    if (g.act == 1) y = silu(y);
+                    else if (g.act == 2) y *= dsilu(aux[c0 + e]);
+                    h[e] = __float2bfloat16(y);
+                }
+                *reinterpret_cast<uint4 *>(oh + c0) = *reinterpret_cast<const uint4 *>(h);
             }
         }
     }
@@ -351,6 +399,12 @@ int fdadi_mlp_gemm(const fdadi_gemm_t *a, void *stream) {
                       a->strideA % 8 == 0 && a->strideB % 8 == 0,
                   "GEMM operands must be 16-byte aligned");
     FDADI_REQUIRE(a->act == 0 || a->act == 1 || (a->act == 2 && a->aux), "bad GEMM epilogue");
+    FDADI_REQUIRE(!a->out_f32 || ((uintptr_t)a->out_f32 % 16 == 0 && a->ldo % 4 == 0 &&
+                                  a->strideO % 4 == 0 && a->ldo >= a->N),
+                  "GEMM fp32 output must be 16-byte aligned with ldo, strideO multiples of 4");
+    FDADI_REQUIRE(!a->out_bf16 || ((uintptr_t)a->out_bf16 % 16 == 0 && a->ldh % 8 == 0 &&
+                                   a->strideH % 8 == 0 && a->ldh >= a->N),
+                  "GEMM bf16 output must be 16-byte aligned with ldh, strideH multiples of 8");
     FDADI_REQUIRE(a->problems >= 1, "GEMM needs at least one problem");
     static bool attr[64] = {false};
     int dev = 0;
