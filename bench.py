@@ -267,7 +267,7 @@ def plain_vs_batched(torch, n_batch=2048):
     torch.cuda.synchronize()
     plain = reps / (time.perf_counter() - t0)
     b = HestonBatch([opt] * n_batch, [(S, v)] * n_batch, scheme="douglas", n_steps=n - 1, dt=dt,
-                    theta=0.5, implicit_steps=2, implicit_dt_factor=0.5, graph=True)
+                    theta=0.5, implicit_steps=2, implicit_dt_factor=0.5, graph=True, plan="auto")
     V0 = b.pack([grid_host] * n_batch)
     V = torch.empty_like(V0)
     idx = b.flat_index()
@@ -292,7 +292,7 @@ def plain_vs_batched(torch, n_batch=2048):
     p_batch = float(out[0].item())
     return {"config": "150x150, nt=150, 2 implicit half-steps + Douglas theta=0.5",
             "plain_options_per_s": plain, "batched_options_per_s": batched,
-            "ratio": batched / plain, "batch": n_batch,
+            "ratio": batched / plain, "batch": n_batch, "plan": b.plan,
             "price_plain": p_plain, "price_batched": p_batch,
             "price_rel_diff": abs(p_plain - p_batch) / abs(p_plain)}
 
@@ -540,6 +540,8 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=32)
     ap.add_argument("--cpu-sample", type=int, default=32)
     ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="line-solve launch plan from the size heuristic, not the autotuner")
     ap.add_argument("--workload", default="batch", choices=["batch", "config2", "surrogate", "gemm"])
     ap.add_argument("--train", type=int, default=1 << 17)
     ap.add_argument("--test", type=int, default=1 << 13)
@@ -579,8 +581,11 @@ def main():
     params = params_of(w)
     nt = w["nt"]
     dts = (w["T"] / nt).tolist()
+    t_tune = time.perf_counter()
     batch = HestonBatch(params, meshes, scheme="hv", n_steps=nt - 1, dt=dts, theta=HV_THETA,
-                        implicit_steps=2, implicit_dt_factor=0.5, graph=True)
+                        implicit_steps=2, implicit_dt_factor=0.5, graph=True,
+                        plan=None if args.no_tune else "auto")
+    t_tune = time.perf_counter() - t_tune
     # device-resident inputs (value) and pinned host copies (e2e)
     V0_dev = batch.pack(payoffs(w, meshes))
     V = torch.empty_like(V0_dev)
@@ -684,6 +689,8 @@ def main():
                              "peak_source": "measured live (fdadi_fp64_probe)",
                              "flops_per_point": STAGE_FLOPS[dom]},
                "stage_ms": {k: round(v[0], 4) for k, v in st.items()},
+               "plan": dict(batch.plan, tuned=not args.no_tune,
+                            setup_s=round(t_tune, 2)),
                "clocks": clk}
         if args.cpu_sample > 0:
             out["cpu_baseline"] = cpu_baseline(

@@ -41,6 +41,22 @@ class Mixed(ctypes.Structure):
                 ("R", ctypes.c_void_p)]
 
 
+class HestonPlan(ctypes.Structure):
+    """fdadi_heston_plan_t"""
+    _fields_ = [("spot_kind", ctypes.c_int32), ("spot_a", ctypes.c_int32),
+                ("spot_b", ctypes.c_int32), ("var_kind", ctypes.c_int32),
+                ("var_warps", ctypes.c_int32), ("reserved", ctypes.c_int32 * 3)]
+
+    FIELDS = ("spot_kind", "spot_a", "spot_b", "var_kind", "var_warps")
+
+    def as_dict(self):
+        return {k: int(getattr(self, k)) for k in self.FIELDS}
+
+    @classmethod
+    def from_dict(cls, d):
+        return cls(*[int(d[k]) for k in cls.FIELDS])
+
+
 class HestonBatch(ctypes.Structure):
     """fdadi_heston_batch_t"""
     _fields_ = [("n_options", ctypes.c_int32), ("scheme", ctypes.c_int32),
@@ -51,7 +67,7 @@ class HestonBatch(ctypes.Structure):
                 ("n0", ctypes.c_void_p), ("n1", ctypes.c_void_p),
                 ("spots", ctypes.c_void_p), ("vars", ctypes.c_void_p),
                 ("params", ctypes.c_void_p), ("dt", ctypes.c_void_p),
-                ("barrier", ctypes.c_void_p)]
+                ("barrier", ctypes.c_void_p), ("plan", ctypes.c_void_p)]
 
 
 class Gemm(ctypes.Structure):
@@ -99,6 +115,11 @@ SIGNATURES = {
     "fdadi_gather": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                     ctypes.c_int64, ctypes.c_void_p]),
     "fdadi_heston_launch_count": (ctypes.c_int64, [ctypes.POINTER(HestonBatch)]),
+    "fdadi_heston_tune": (ctypes.c_int, [ctypes.POINTER(HestonBatch), ctypes.c_void_p,
+                                         ctypes.c_int64, ctypes.c_int32,
+                                         ctypes.POINTER(HestonPlan), ctypes.c_void_p]),
+    "fdadi_heston_default_plan": (ctypes.c_int, [ctypes.POINTER(HestonBatch),
+                                                 ctypes.POINTER(HestonPlan)]),
     "fdadi_heston_stage": (ctypes.c_int, [ctypes.POINTER(HestonBatch), ctypes.c_void_p,
                                           ctypes.c_int64, ctypes.c_void_p, ctypes.c_int32,
                                           ctypes.c_void_p]),

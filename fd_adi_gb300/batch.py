@@ -8,6 +8,9 @@ reference prices one option per engine with dozens of launches per step
 beyond the per-option results, which match the reference CPU engine.
 """
 import ctypes
+import hashlib
+import json
+import os
 
 import numpy as np
 import torch
@@ -18,6 +21,51 @@ from . import mesh as _mesh
 SCHEMES = {"douglas": _lib.SCHEME_DOUGLAS, "hv": _lib.SCHEME_HV,
            "hundsdorferverwer": _lib.SCHEME_HV}
 HV_THETA = 0.5 + np.sqrt(3.0) / 6.0
+
+
+# Launch shapes the engine implements (fdadi_heston_plan_t fields): spot solve
+# (kind 0: line per thread, rows prefetched, threads per block; kind 1:
+# partitioned lines, lines per block, segments per line) and variance solve
+# (kind 0: one tile per warp; kind 1: two tiles, pipelined copies; warps per block).
+SPOT_PLANS = [(0, 1, 128), (0, 1, 64), (0, 1, 256), (0, 4, 32), (0, 8, 32), (0, 8, 64),
+              (1, 32, 4), (1, 32, 8), (1, 32, 16), (1, 32, 32), (1, 16, 16), (1, 16, 32),
+              (1, 16, 64), (1, 8, 32), (1, 8, 64), (1, 8, 128)]
+VAR_PLANS = [(0, 4), (0, 2), (1, 1), (1, 2), (1, 4)]
+
+
+def make_plan(spot, var):
+    """Plan dict from a SPOT_PLANS and a VAR_PLANS entry."""
+    return {"spot_kind": spot[0], "spot_a": spot[1], "spot_b": spot[2],
+            "var_kind": var[0], "var_warps": var[1]}
+
+
+# Tuned launch plans by batch shape (this process); FDADI_TUNE_CACHE names a
+# JSON file that keeps them across processes.
+_PLANS = {}
+
+
+def _cache_path():
+    return os.environ.get("FDADI_TUNE_CACHE")
+
+
+def _load_plans():
+    path = _cache_path()
+    if path and os.path.exists(path):
+        try:
+            with open(path) as f:
+                for k, v in json.load(f).items():
+                    _PLANS.setdefault(k, v)
+        except (OSError, ValueError):
+            pass
+
+
+def _save_plans():
+    path = _cache_path()
+    if path:
+        tmp = path + ".tmp"
+        with open(tmp, "w") as f:
+            json.dump(_PLANS, f, indent=1, sort_keys=True)
+        os.replace(tmp, path)
 
 
 def option_params(opt):
@@ -35,11 +83,14 @@ class HestonBatch(object):
     meshes:  list of (spots, vars) numpy arrays, one per option.
     dt:      per-option main step (scalar or sequence).
     Schedule: ``implicit_steps`` fully implicit steps of dt*implicit_dt_factor,
-    then ``n_steps`` of ``scheme`` ("douglas" or "hv") at ``theta``."""
+    then ``n_steps`` of ``scheme`` ("douglas" or "hv") at ``theta``.
+    plan:    launch plan of the line solves: None (size heuristic), "auto"
+             (measured by the autotuner on this batch, cached by batch shape)
+             or a dict of fdadi_heston_plan_t fields."""
 
     def __init__(self, options, meshes, scheme="hv", n_steps=1, dt=0.01, theta=HV_THETA,
                  implicit_steps=0, implicit_dt_factor=0.5, barrier=None, drop_zero_mixed=True,
-                 graph=False, device=None, stream=None):
+                 graph=False, device=None, stream=None, plan=None):
         self.device = device or torch.device("cuda", torch.cuda.current_device())
         n = len(options)
         if n == 0 or len(meshes) != n:
@@ -75,7 +126,8 @@ class HestonBatch(object):
             float(implicit_dt_factor), flags, 0,
             self._n0_host.ctypes.data, self._n1_host.ctypes.data,
             self.spots.data_ptr(), self.vars.data_ptr(), self.params.data_ptr(),
-            self.dt.data_ptr(), self.barrier.data_ptr())
+            self.dt.data_ptr(), self.barrier.data_ptr(), None)
+        self._plan = None
         lib = _lib.load()
         nbytes = lib.fdadi_heston_workspace_bytes(ctypes.byref(self.struct))
         if nbytes < 0:
@@ -83,6 +135,49 @@ class HestonBatch(object):
         self.workspace_bytes = int(nbytes)
         self.workspace = torch.empty(self.workspace_bytes, dtype=torch.uint8, device=dev)
         self._prepare()
+        if isinstance(plan, str):
+            if plan != "auto":
+                raise ValueError("plan must be None, 'auto' or a dict")
+            self.tune()
+        elif plan is not None:
+            self.set_plan(plan)
+
+    @property
+    def shape_key(self):
+        """Key of the batch shape the launch plan depends on."""
+        h = hashlib.sha1(self.n0.tobytes() + self.n1.tobytes()).hexdigest()[:16]
+        return "%d:%d:%s" % (self.n, self.total_points, h)
+
+    def set_plan(self, plan):
+        """Use this launch plan (dict of fdadi_heston_plan_t fields) from now on."""
+        self._plan = _lib.HestonPlan.from_dict(plan)
+        self.struct.plan = ctypes.cast(ctypes.pointer(self._plan), ctypes.c_void_p)
+
+    @property
+    def plan(self):
+        """The launch plan in use (the size heuristic's when none was set)."""
+        if self._plan is not None:
+            return self._plan.as_dict()
+        p = _lib.HestonPlan()
+        _lib.call("fdadi_heston_default_plan", ctypes.byref(self.struct), ctypes.byref(p))
+        return p.as_dict()
+
+    def tune(self, reps=3, force=False):
+        """Measure every launch plan of the line solves on this batch and keep
+        the fastest (cached by batch shape). Overwrites the stage buffers
+        only; the state is untouched."""
+        _load_plans()
+        key = self.shape_key
+        if force or key not in _PLANS:
+            p = _lib.HestonPlan()
+            with torch.cuda.stream(self.stream):
+                _lib.call("fdadi_heston_tune", ctypes.byref(self.struct),
+                          ctypes.c_void_p(self.workspace.data_ptr()), self.workspace_bytes,
+                          int(reps), ctypes.byref(p), self._sptr())
+            _PLANS[key] = p.as_dict()
+            _save_plans()
+        self.set_plan(_PLANS[key])
+        return self.plan
 
     @classmethod
     def from_options(cls, options, nspots, nvols, spot_max_factor=8.0, var_max=5.0,

@@ -53,8 +53,7 @@ constexpr int EXPL_THREADS = TI * TJ;
 constexpr int XR = TI + 2;            // staged rows (one-row halo above and below)
 constexpr int XC = TJ + 3;            // staged columns (two on the left, one on the right)
 constexpr int XCP = 36;               // padded row pitch of the staged tile
-constexpr int SOLVE_THREADS = 128;
-constexpr int VS_WARPS = 4;           // warps per variance-solve block
+constexpr int SPOT_MAX_THREADS = 256; // largest block of the line-per-thread spot solve
 constexpr int VS_PITCH = 33;          // padded pitch of the 32x32 variance tile
 
 // Device view of a prepared workspace.
@@ -457,7 +456,7 @@ __global__ void __launch_bounds__(EXPL_THREADS) explicit_kernel(Arena A, const d
 // IMPLICIT: implicit-plan factors and residual. SUBT: write x - T (the next
 // stage's right-hand side) instead of x.
 template <bool IMPLICIT, bool SUBT, int PF>
-__global__ void __launch_bounds__(SOLVE_THREADS) spot_solve_kernel(Arena A, const double *src,
+__global__ void __launch_bounds__(SPOT_MAX_THREADS) spot_solve_kernel(Arena A, const double *src,
                                                                    double *dst) {
     const int64_t line = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (line >= A.SV) return;
@@ -564,12 +563,12 @@ __global__ void __launch_bounds__(SOLVE_THREADS) spot_solve_kernel(Arena A, cons
 // (coalesced) into a padded shared tile, each lane runs its row's recurrence
 // over the chunk, and the chunk is stored back row by row. The bottom row of
 // the right-hand side is folded with the option's fold factor.
-template <bool IMPLICIT>
-__global__ void __launch_bounds__(VS_WARPS * 32) var_solve_kernel(Arena A, int n_tasks,
-                                                                  const double *src, double *dst) {
-    __shared__ double tile[VS_WARPS][32][VS_PITCH];
+template <bool IMPLICIT, int NW>
+__global__ void __launch_bounds__(NW * 32) var_solve_kernel(Arena A, int n_tasks,
+                                                            const double *src, double *dst) {
+    __shared__ double tile[NW][32][VS_PITCH];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int task = blockIdx.x * VS_WARPS + warp;
+    const int task = blockIdx.x * NW + warp;
     if (task >= n_tasks) return;
     const int4 tk = A.vtasks[task];
     const int o = tk.x, i0 = tk.y, rows = tk.z;
@@ -627,6 +626,246 @@ __global__ void __launch_bounds__(VS_WARPS * 32) var_solve_kernel(Arena A, int n
         for (int rr = 0; rr < rows; ++rr)
             if (lane < w) dst[base + (int64_t)rr * n1 + c0 + lane] = tl[rr][lane];
         __syncwarp();
+    }
+}
+
+// Partitioned spot solve, for batches with few, long spot lines (one large
+// grid, small batches), where one thread per line leaves most of the GPU idle.
+// A block holds LPB adjacent lines (thread t: line t % LPB) and cuts each line
+// into NSEG contiguous row segments (segment t / LPB), so accesses stay
+// coalesced across the block's lines. Both Thomas sweeps are first-order
+// linear recurrences on the precomputed factors,
+//   d_i = (r_i - a_i d_{i-1}) / m_i,   x_i = d_i - c'_i x_{i+1},
+// so each segment runs them from a zero carry while tracking the product of
+// the multipliers (the carry's weight), one thread per line combines the
+// segment carries in order, and a second pass adds weight * carry: four
+// passes of a segment instead of two passes of the whole line.
+template <bool IMPLICIT, bool SUBT, int LPB, int NSEG>
+__global__ void __launch_bounds__(LPB * NSEG) spot_seg_kernel(Arena A, const double *src,
+                                                              double *dst) {
+    __shared__ double cval[NSEG][LPB], cwt[NSEG][LPB];
+    const int t = threadIdx.x, ls = t % LPB, sg = t / LPB;
+    const int64_t line = (int64_t)blockIdx.x * LPB + ls;
+    const bool valid = line < A.SV;
+    const double *L = IMPLICIT ? A.LSi : A.LS;
+    const int64_t P = A.P;
+    int o = 0, n0 = 0, n1 = 1, lo = 0, hi = 0;
+    int64_t b = 0;
+    if (valid) {
+        o = A.lineS[line];
+        n0 = A.n0[o];
+        n1 = A.n1[o];
+        b = A.p_off[o] + (line - A.v_off[o]);
+        const int seg = (n0 + NSEG - 1) / NSEG;
+        lo = min(n0, sg * seg);
+        hi = min(n0, lo + seg);
+    }
+    // pass 1: forward sweep from a zero carry; g = d(d_i)/d(d_{lo-1})
+    {
+        const int fl = valid ? A.oflags[o] : 0;
+        const bool slow = fl & OPT_S_LOW_DIR, shigh = fl & OPT_S_HIGH_DIR;
+        const double gl = valid ? A.dirS[line] : 0.0, gh = valid ? A.dirS[A.SV + line] : 0.0;
+        double d = 0.0, g = 1.0;
+        for (int i = lo; i < hi; ++i) {
+            const int64_t p = b + (int64_t)i * n1;
+            double rk;
+            if (i == 0 && slow) rk = gl;
+            else if (i == n0 - 1 && shigh) rk = gh;
+            else rk = src[p];
+            if (IMPLICIT && i == n0 - 1) rk = rk - A.RSi[line];
+            const double inv = L[P + p];
+            if (i == 0) {
+                d = rk * inv;
+                g = 0.0;
+            } else {
+                const double a = L[p];
+                d = (rk - a * d) * inv;
+                g = (-a * g) * inv;
+            }
+            dst[p] = d;
+        }
+        cval[sg][ls] = d;
+        cwt[sg][ls] = g;
+    }
+    __syncthreads();
+    if (sg == 0) {
+        double D = 0.0;  // d at the row before segment s
+        for (int s = 0; s < NSEG; ++s) {
+            const double v = cval[s][ls], w = cwt[s][ls];
+            cval[s][ls] = D;
+            D = fma(w, D, v);
+        }
+    }
+    __syncthreads();
+    // pass 2: d_i += g_i * carry (segment 0 starts at row 0 and is exact)
+    if (sg > 0) {
+        const double C = cval[sg][ls];
+        double g = 1.0;
+        for (int i = lo; i < hi; ++i) {
+            const int64_t p = b + (int64_t)i * n1;
+            g = (-L[p] * g) * L[P + p];
+            dst[p] = fma(g, C, dst[p]);
+        }
+    }
+    __syncthreads();
+    // pass 3: back substitution from a zero carry; h = d(x_i)/d(x_{hi})
+    {
+        double x = 0.0, h = 1.0;
+        for (int i = hi - 1; i >= lo; --i) {
+            const int64_t p = b + (int64_t)i * n1;
+            if (i == n0 - 1) {
+                x = dst[p];
+                h = 0.0;
+            } else {
+                const double c = L[2 * P + p];
+                x = dst[p] - c * x;
+                h = -c * h;
+            }
+            dst[p] = x;
+        }
+        cval[sg][ls] = x;
+        cwt[sg][ls] = h;
+    }
+    __syncthreads();
+    if (sg == 0) {
+        double X = 0.0;  // x at the row after segment s
+        for (int s = NSEG - 1; s >= 0; --s) {
+            const double v = cval[s][ls], w = cwt[s][ls];
+            cval[s][ls] = X;
+            X = fma(w, X, v);
+        }
+    }
+    __syncthreads();
+    // pass 4: x_i += h_i * carry, then the stage's output
+    {
+        const double C = cval[sg][ls];
+        const double th = (SUBT && valid) ? A.theta[o] : 0.0;
+        double h = 1.0;
+        for (int i = hi - 1; i >= lo; --i) {
+            const int64_t p = b + (int64_t)i * n1;
+            h = (i == n0 - 1) ? 0.0 : -L[2 * P + p] * h;
+            const double x = fma(h, C, dst[p]);
+            dst[p] = SUBT ? fma(-th, A.T[p], x) : x;
+        }
+    }
+}
+
+__device__ __forceinline__ void cp_async8(void *sdst, const void *gsrc) {
+    const uint32_t s = (uint32_t)__cvta_generic_to_shared(sdst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(s), "l"(gsrc));
+}
+
+// Variance-line solve, pipelined: as var_solve_kernel (one warp per task of up
+// to 32 grid rows, 32x32 chunks through a padded shared tile), with two tiles
+// per warp so the cp.async copies of the next chunk are in flight while the
+// lanes run the current chunk's recurrence, and each chunk's Thomas factors
+// held one per lane and broadcast by shuffle (no global load on the
+// recurrence's path). The back substitution starts from the forward sweep's
+// last chunk, still in shared memory. Dynamic shared memory:
+// NW * 2 * 32 * VS_PITCH doubles.
+template <bool IMPLICIT, int NW>
+__global__ void __launch_bounds__(NW * 32) var_solve_pipe_kernel(Arena A, int n_tasks,
+                                                                 const double *src, double *dst) {
+    extern __shared__ double vsm[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int task = blockIdx.x * NW + warp;
+    if (task >= n_tasks) return;
+    double(*tl)[32][VS_PITCH] =
+        reinterpret_cast<double(*)[32][VS_PITCH]>(vsm + (size_t)warp * 2 * 32 * VS_PITCH);
+    const int4 tk = A.vtasks[task];
+    const int o = tk.x, i0 = tk.y, rows = tk.z;
+    const int n1 = A.n1[o];
+    const int64_t base = A.p_off[o] + (int64_t)i0 * n1;
+    const int64_t vo = A.v_off[o], SV = A.SV;
+    const double *L = IMPLICIT ? A.LVvi : A.LVv;
+    const double f = IMPLICIT ? A.foldVi[o] : A.foldV[o];
+    const double z = IMPLICIT ? A.LVzi[o] : A.LVz[o];
+    const bool special = (i0 + lane == 0) && (A.oflags[o] & OPT_ROW0_ZERO);
+    const int nch = (n1 + 31) >> 5;
+    const unsigned FULL = 0xffffffffu;
+    auto issue = [&](const double *from, int ch, int buf) {
+        const int c0 = ch << 5, w = min(32, n1 - c0);
+        if (lane < w)
+            for (int rr = 0; rr < rows; ++rr)
+                cp_async8(&tl[buf][rr][lane], from + base + (int64_t)rr * n1 + c0 + lane);
+        asm volatile("cp.async.commit_group;");
+    };
+    // forward sweep
+    issue(src, 0, 0);
+    double fa = 0.0, fi = 0.0;
+    if (lane < min(32, n1)) { fa = L[vo + lane]; fi = L[SV + vo + lane]; }
+    double dp = 0.0, rprev = 0.0;
+    for (int ch = 0; ch < nch; ++ch) {
+        const int buf = ch & 1, c0 = ch << 5, w = min(32, n1 - c0);
+        double na = 0.0, ni = 0.0;
+        if (ch + 1 < nch) {
+            issue(src, ch + 1, buf ^ 1);
+            const int c1 = c0 + 32;
+            if (lane < min(32, n1 - c1)) { na = L[vo + c1 + lane]; ni = L[SV + vo + c1 + lane]; }
+            asm volatile("cp.async.wait_group 1;");
+        } else {
+            asm volatile("cp.async.wait_group 0;");
+        }
+        __syncwarp();
+        for (int c = 0; c < w; ++c) {
+            const double ac = __shfl_sync(FULL, fa, c), ic = __shfl_sync(FULL, fi, c);
+            if (lane < rows) {
+                const int col = c0 + c;
+                double rk = tl[buf][lane][c];
+                const double raw = rk;
+                if (special) {
+                    dp = rk * z;
+                } else {
+                    if (col == n1 - 1) rk += 1.0 * rprev * f;
+                    dp = (col == 0) ? rk * ic : (rk - ac * dp) * ic;
+                }
+                tl[buf][lane][c] = dp;
+                rprev = raw;
+            }
+        }
+        __syncwarp();
+        if (lane < w)
+            for (int rr = 0; rr < rows; ++rr)
+                dst[base + (int64_t)rr * n1 + c0 + lane] = tl[buf][rr][lane];
+        __syncwarp();
+        fa = na;
+        fi = ni;
+    }
+    // the next copies read dst back: order this lane's stores before them
+    __threadfence_block();
+    // back substitution, last chunk first (already in buf (nch-1) & 1)
+    double fc = 0.0;
+    {
+        const int c0 = (nch - 1) << 5;
+        if (lane < n1 - c0) fc = L[2 * SV + vo + c0 + lane];
+    }
+    double x = 0.0;
+    for (int ch = nch - 1; ch >= 0; --ch) {
+        const int buf = ch & 1, c0 = ch << 5, w = min(32, n1 - c0);
+        double nc = 0.0;
+        if (ch > 0) {
+            issue(dst, ch - 1, buf ^ 1);
+            nc = L[2 * SV + vo + c0 - 32 + lane];
+            asm volatile("cp.async.wait_group 1;");
+        } else {
+            asm volatile("cp.async.wait_group 0;");
+        }
+        __syncwarp();
+        for (int c = w - 1; c >= 0; --c) {
+            const double cc = __shfl_sync(FULL, fc, c);
+            if (lane < rows) {
+                const int col = c0 + c;
+                const double d = tl[buf][lane][c];
+                x = (col == n1 - 1 || special) ? d : d - cc * x;
+                tl[buf][lane][c] = x;
+            }
+        }
+        __syncwarp();
+        if (lane < w)
+            for (int rr = 0; rr < rows; ++rr)
+                dst[base + (int64_t)rr * n1 + c0 + lane] = tl[buf][rr][lane];
+        __syncwarp();
+        fc = nc;
     }
 }
 
@@ -750,25 +989,135 @@ static Arena arena_view(const Layout &L, char *ws) {
     return A;
 }
 
-// Launch shape of the spot solve, chosen per batch: with many lines, thread
-// parallelism hides memory latency and the plain loop (fewer registers, more
-// resident threads) is fastest; with few lines (one large grid, small
-// batches) each thread prefetches rows ahead and 32-thread blocks spread the
-// lines over more SMs.
+// ---- launch plans ----------------------------------------------------------
+//
+// The spot and variance solves come in several launch shapes; which is
+// fastest depends on the batch (number and length of lines, grid sizes), so a
+// plan names one shape of each and fdadi_heston_tune measures them all on the
+// prepared batch. Without a plan a size heuristic picks: with many spot lines,
+// thread parallelism hides memory latency and the plain loop (fewer registers,
+// more resident threads) wins; with few lines the prefetching loop in 32-thread
+// blocks spreads them over more SMs.
+
+using SpotFn = void (*)(Arena, const double *, double *);
+using VarFn = void (*)(Arena, int, const double *, double *);
+
+struct SpotVariant {
+    int kind, a, b;   // plan fields
+    int threads;      // block size
+    int lines;        // spot lines per block
+    SpotFn main;      // main plan, writes x - theta T
+    SpotFn impl;      // implicit plan
+};
+struct VarVariant {
+    int kind, warps;
+    int smem;         // dynamic shared memory bytes
+    VarFn main, impl;
+};
+
+#define SPOT_T(PF, TH)                                                                  \
+    SpotVariant{0, PF, TH, TH, TH, spot_solve_kernel<false, true, PF>,                  \
+                spot_solve_kernel<true, false, PF>}
+#define SPOT_S(LPB, NS)                                                                 \
+    SpotVariant{1, LPB, NS, LPB * NS, LPB, spot_seg_kernel<false, true, LPB, NS>,       \
+                spot_seg_kernel<true, false, LPB, NS>}
+static const SpotVariant SPOT_VARIANTS[] = {
+    SPOT_T(1, 128), SPOT_T(1, 64),  SPOT_T(1, 256), SPOT_T(4, 32),  SPOT_T(8, 32),
+    SPOT_T(8, 64),  SPOT_S(32, 4),  SPOT_S(32, 8),  SPOT_S(32, 16), SPOT_S(32, 32),
+    SPOT_S(16, 16), SPOT_S(16, 32), SPOT_S(16, 64), SPOT_S(8, 32),  SPOT_S(8, 64),
+    SPOT_S(8, 128)};
+#undef SPOT_T
+#undef SPOT_S
+
+constexpr int VAR_PIPE_SMEM_PER_WARP = 2 * 32 * VS_PITCH * (int)sizeof(double);
+static const VarVariant VAR_VARIANTS[] = {
+    {0, 4, 0, var_solve_kernel<false, 4>, var_solve_kernel<true, 4>},
+    {0, 2, 0, var_solve_kernel<false, 2>, var_solve_kernel<true, 2>},
+    {1, 1, VAR_PIPE_SMEM_PER_WARP, var_solve_pipe_kernel<false, 1>, var_solve_pipe_kernel<true, 1>},
+    {1, 2, 2 * VAR_PIPE_SMEM_PER_WARP, var_solve_pipe_kernel<false, 2>,
+     var_solve_pipe_kernel<true, 2>},
+    {1, 4, 4 * VAR_PIPE_SMEM_PER_WARP, var_solve_pipe_kernel<false, 4>,
+     var_solve_pipe_kernel<true, 4>}};
+
+constexpr int N_SPOT_VARIANTS = sizeof(SPOT_VARIANTS) / sizeof(SPOT_VARIANTS[0]);
+constexpr int N_VAR_VARIANTS = sizeof(VAR_VARIANTS) / sizeof(VAR_VARIANTS[0]);
 constexpr int64_t SPOT_MANY_LINES = 150000;
+
+static int find_spot(int kind, int a, int b) {
+    for (int k = 0; k < N_SPOT_VARIANTS; ++k)
+        if (SPOT_VARIANTS[k].kind == kind && SPOT_VARIANTS[k].a == a && SPOT_VARIANTS[k].b == b)
+            return k;
+    return -1;
+}
+static int find_var(int kind, int warps) {
+    for (int k = 0; k < N_VAR_VARIANTS; ++k)
+        if (VAR_VARIANTS[k].kind == kind && VAR_VARIANTS[k].warps == warps) return k;
+    return -1;
+}
+
+// Dynamic shared memory above 48 KB needs a per-kernel opt-in, once per device.
+static int var_smem_optin() {
+    static std::mutex mu;
+    static bool done[64] = {false};
+    int dev = 0;
+    FDADI_CUDA(cudaGetDevice(&dev));
+    FDADI_REQUIRE(dev >= 0 && dev < 64, "device ordinal out of range");
+    std::lock_guard<std::mutex> g(mu);
+    if (!done[dev]) {
+        for (int k = 0; k < N_VAR_VARIANTS; ++k) {
+            const VarVariant &v = VAR_VARIANTS[k];
+            if (v.smem > 48 * 1024) {
+                FDADI_CUDA(cudaFuncSetAttribute(v.main, cudaFuncAttributeMaxDynamicSharedMemorySize, v.smem));
+                FDADI_CUDA(cudaFuncSetAttribute(v.impl, cudaFuncAttributeMaxDynamicSharedMemorySize, v.smem));
+            }
+        }
+        done[dev] = true;
+    }
+    return FDADI_OK;
+}
+
+static fdadi_heston_plan_t default_plan(const Layout &L) {
+    fdadi_heston_plan_t p{};
+    p.spot_kind = 0;
+    p.spot_a = L.SV >= SPOT_MANY_LINES ? 1 : 8;
+    p.spot_b = L.SV >= SPOT_MANY_LINES ? 128 : 32;
+    p.var_kind = 0;
+    p.var_warps = 4;
+    return p;
+}
 
 struct Grids {
     unsigned tiles, spot, var;
     int n_vtasks;
-    bool many;       // plain-loop spot solve
-    int spot_threads;
+    int si, vi;       // variant indices
 };
 
-static Grids grids(const Layout &L) {
-    const bool many = L.SV >= SPOT_MANY_LINES;
-    const int st = many ? SOLVE_THREADS : 32;
-    return Grids{(unsigned)L.n_tiles, (unsigned)((L.SV + st - 1) / st),
-                 (unsigned)((L.n_vtasks + VS_WARPS - 1) / VS_WARPS), (int)L.n_vtasks, many, st};
+static int grids(const fdadi_heston_batch_t *b, const Layout &L, Grids &g) {
+    const fdadi_heston_plan_t p = b->plan ? *b->plan : default_plan(L);
+    g.si = find_spot(p.spot_kind, p.spot_a, p.spot_b);
+    g.vi = find_var(p.var_kind, p.var_warps);
+    FDADI_REQUIRE(g.si >= 0, "unknown spot-solve plan (%d, %d, %d)", p.spot_kind, p.spot_a,
+                  p.spot_b);
+    FDADI_REQUIRE(g.vi >= 0, "unknown variance-solve plan (%d, %d)", p.var_kind, p.var_warps);
+    const SpotVariant &sv = SPOT_VARIANTS[g.si];
+    const VarVariant &vv = VAR_VARIANTS[g.vi];
+    g.tiles = (unsigned)L.n_tiles;
+    g.spot = (unsigned)((L.SV + sv.lines - 1) / sv.lines);
+    g.var = (unsigned)((L.n_vtasks + vv.warps - 1) / vv.warps);
+    g.n_vtasks = (int)L.n_vtasks;
+    if (vv.smem > 48 * 1024) return var_smem_optin();
+    return FDADI_OK;
+}
+
+static void launch_spot(const Grids &g, bool implicit, const Arena &A, const double *src,
+                        double *dst, cudaStream_t st) {
+    const SpotVariant &v = SPOT_VARIANTS[g.si];
+    (implicit ? v.impl : v.main)<<<g.spot, v.threads, 0, st>>>(A, src, dst);
+}
+static void launch_var(const Grids &g, bool implicit, const Arena &A, const double *src,
+                       double *dst, cudaStream_t st) {
+    const VarVariant &v = VAR_VARIANTS[g.vi];
+    (implicit ? v.impl : v.main)<<<g.var, v.warps * 32, v.smem, st>>>(A, g.n_vtasks, src, dst);
 }
 
 static void launch_stage(int stage, const Grids &g, const Arena &A, double *V, cudaStream_t st) {
@@ -781,20 +1130,11 @@ static void launch_stage(int stage, const Grids &g, const Arena &A, double *V, c
         explicit_kernel<ST_HV3><<<g.tiles, EXPL_THREADS, 0, st>>>(A, V); break;
     case FDADI_STAGE_EXPLICIT_IMPLICIT:
         explicit_kernel<ST_IMPLICIT><<<g.tiles, EXPL_THREADS, 0, st>>>(A, V); break;
-    case FDADI_STAGE_SPOT_SOLVE:
-        if (g.many) spot_solve_kernel<false, true, 1><<<g.spot, g.spot_threads, 0, st>>>(A, A.W, A.W);
-        else spot_solve_kernel<false, true, 8><<<g.spot, g.spot_threads, 0, st>>>(A, A.W, A.W);
-        break;
-    case FDADI_STAGE_VAR_SOLVE_TO_Y2:
-        var_solve_kernel<false><<<g.var, VS_WARPS * 32, 0, st>>>(A, g.n_vtasks, A.W, A.Y2); break;
-    case FDADI_STAGE_VAR_SOLVE_TO_V:
-        var_solve_kernel<false><<<g.var, VS_WARPS * 32, 0, st>>>(A, g.n_vtasks, A.W, V); break;
-    case FDADI_STAGE_VAR_SOLVE_IMPLICIT:
-        var_solve_kernel<true><<<g.var, VS_WARPS * 32, 0, st>>>(A, g.n_vtasks, A.W, A.W); break;
-    case FDADI_STAGE_SPOT_SOLVE_IMPLICIT:
-        if (g.many) spot_solve_kernel<true, false, 1><<<g.spot, g.spot_threads, 0, st>>>(A, A.W, V);
-        else spot_solve_kernel<true, false, 8><<<g.spot, g.spot_threads, 0, st>>>(A, A.W, V);
-        break;
+    case FDADI_STAGE_SPOT_SOLVE: launch_spot(g, false, A, A.W, A.W, st); break;
+    case FDADI_STAGE_VAR_SOLVE_TO_Y2: launch_var(g, false, A, A.W, A.Y2, st); break;
+    case FDADI_STAGE_VAR_SOLVE_TO_V: launch_var(g, false, A, A.W, V, st); break;
+    case FDADI_STAGE_VAR_SOLVE_IMPLICIT: launch_var(g, true, A, A.W, A.W, st); break;
+    case FDADI_STAGE_SPOT_SOLVE_IMPLICIT: launch_spot(g, true, A, A.W, V, st); break;
     default: break;
     }
 }
@@ -803,7 +1143,9 @@ static void launch_stage(int stage, const Grids &g, const Arena &A, double *V, c
 // capture).
 static int launch_steps(const fdadi_heston_batch_t *b, const Layout &L, const Arena &A, double *V,
                         cudaStream_t st) {
-    const Grids g = grids(L);
+    Grids g;
+    const int rc = grids(b, L, g);
+    if (rc) return rc;
     for (int s = 0; s < b->implicit_steps; ++s) {
         launch_stage(FDADI_STAGE_EXPLICIT_IMPLICIT, g, A, V, st);
         launch_stage(FDADI_STAGE_VAR_SOLVE_IMPLICIT, g, A, V, st);
@@ -832,10 +1174,12 @@ static int launch_steps(const fdadi_heston_batch_t *b, const Layout &L, const Ar
 struct GraphKey {
     const void *ws; const void *V; int n_opt, scheme, n_steps, smoothing;
     int64_t P, SS, SV, n_tiles, n_vtasks;
+    int si, vi;
     bool operator==(const GraphKey &o) const {
         return ws == o.ws && V == o.V && n_opt == o.n_opt && scheme == o.scheme &&
                n_steps == o.n_steps && smoothing == o.smoothing && P == o.P && SS == o.SS &&
-               SV == o.SV && n_tiles == o.n_tiles && n_vtasks == o.n_vtasks;
+               SV == o.SV && n_tiles == o.n_tiles && n_vtasks == o.n_vtasks && si == o.si &&
+               vi == o.vi;
     }
 };
 struct GraphKeyHash {
@@ -935,8 +1279,11 @@ int fdadi_heston_run(const fdadi_heston_batch_t *b, void *workspace, int64_t ws_
     Arena A = arena_view(L, (char *)workspace);
     if (!(b->flags & FDADI_HESTON_GRAPH)) return launch_steps(b, L, A, V, st);
     FDADI_REQUIRE(st != nullptr, "graph mode needs a non-default stream");
+    Grids g;
+    rc = grids(b, L, g);
+    if (rc) return rc;
     GraphKey key{workspace, V, b->n_options, b->scheme, b->n_steps, b->implicit_steps,
-                 L.P, L.SS, L.SV, L.n_tiles, L.n_vtasks};
+                 L.P, L.SS, L.SV, L.n_tiles, L.n_vtasks, g.si, g.vi};
     cudaGraphExec_t exec = nullptr;
     {
         std::lock_guard<std::mutex> g(g_graph_mu);
@@ -977,8 +1324,83 @@ int fdadi_heston_stage(const fdadi_heston_batch_t *b, void *workspace, int64_t w
                     stage == FDADI_STAGE_SPOT_SOLVE_IMPLICIT) || L.smoothing,
                   "stage %d needs a batch with implicit steps", stage);
     Arena A = arena_view(L, (char *)workspace);
-    launch_stage(stage, grids(L), A, V, as_stream(stream));
+    Grids g;
+    rc = grids(b, L, g);
+    if (rc) return rc;
+    launch_stage(stage, g, A, V, as_stream(stream));
     FDADI_CHECK_LAUNCH();
+    return FDADI_OK;
+}
+
+int fdadi_heston_default_plan(const fdadi_heston_batch_t *b, fdadi_heston_plan_t *plan) {
+    Layout L;
+    int rc = make_layout(b, L);
+    if (rc) return rc;
+    FDADI_REQUIRE(plan != nullptr, "null plan");
+    *plan = default_plan(L);
+    return FDADI_OK;
+}
+
+int fdadi_heston_tune(const fdadi_heston_batch_t *b, void *workspace, int64_t ws_bytes,
+                      int32_t reps, fdadi_heston_plan_t *plan, void *stream) {
+    Layout L;
+    int rc = make_layout(b, L);
+    if (rc) return rc;
+    rc = check_ws(L, workspace, ws_bytes);
+    if (rc) return rc;
+    FDADI_REQUIRE(plan != nullptr, "null plan");
+    FDADI_REQUIRE(reps >= 1 && reps <= 1000, "reps must be 1..1000 (%d)", reps);
+    rc = var_smem_optin();
+    if (rc) return rc;
+    cudaStream_t st = as_stream(stream);
+    Arena A = arena_view(L, (char *)workspace);
+    cudaEvent_t e0, e1;
+    FDADI_CUDA(cudaEventCreate(&e0));
+    FDADI_CUDA(cudaEventCreate(&e1));
+    // time one variant: a warm-up launch, then reps launches between events
+    auto time_it = [&](auto launch, float &ms) -> int {
+        launch();
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) { ms = -1.0f; return FDADI_OK; }  // shape not launchable here
+        cudaEventRecord(e0, st);
+        for (int r = 0; r < reps; ++r) launch();
+        cudaEventRecord(e1, st);
+        e = cudaEventSynchronize(e1);
+        if (e != cudaSuccess) {
+            set_error("CUDA error while tuning: %s", cudaGetErrorString(e));
+            return FDADI_E_CUDA;
+        }
+        cudaEventElapsedTime(&ms, e0, e1);
+        return FDADI_OK;
+    };
+    fdadi_heston_plan_t best = default_plan(L);
+    float best_spot = 1e30f, best_var = 1e30f;
+    for (int k = 0; k < N_SPOT_VARIANTS && !rc; ++k) {
+        const SpotVariant &v = SPOT_VARIANTS[k];
+        const unsigned grid = (unsigned)((L.SV + v.lines - 1) / v.lines);
+        float ms = 0.0f;
+        rc = time_it([&] { v.main<<<grid, v.threads, 0, st>>>(A, A.W, A.W); }, ms);
+        if (!rc && ms >= 0.0f && ms < best_spot) {
+            best_spot = ms;
+            best.spot_kind = v.kind; best.spot_a = v.a; best.spot_b = v.b;
+        }
+    }
+    for (int k = 0; k < N_VAR_VARIANTS && !rc; ++k) {
+        const VarVariant &v = VAR_VARIANTS[k];
+        const unsigned grid = (unsigned)((L.n_vtasks + v.warps - 1) / v.warps);
+        const int nt = (int)L.n_vtasks;
+        float ms = 0.0f;
+        rc = time_it([&] { v.main<<<grid, v.warps * 32, v.smem, st>>>(A, nt, A.W, A.W); }, ms);
+        if (!rc && ms >= 0.0f && ms < best_var) {
+            best_var = ms;
+            best.var_kind = v.kind; best.var_warps = v.warps;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    FDADI_REQUIRE(best_spot < 1e30f && best_var < 1e30f, "no launch plan could be launched");
+    *plan = best;
     return FDADI_OK;
 }
 

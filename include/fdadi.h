@@ -160,6 +160,17 @@ int fdadi_axpby(double *y, const double *x, double a, double b, int64_t n, void 
 /* operators built on the device as HestonFiniteDifferenceEngine builds     */
 /* them (FiniteDifferenceEngineGPU.pyx:596-724, heston.py:302-359).         */
 /* ------------------------------------------------------------------------ */
+/* Launch plan of the batched engine's line solves (chosen by
+ * fdadi_heston_tune, or by a size heuristic when a batch has none). */
+typedef struct fdadi_heston_plan {
+    int32_t spot_kind;   /* 0: one thread per spot line; 1: partitioned lines */
+    int32_t spot_a;      /* kind 0: rows prefetched ahead (1, 4 or 8); kind 1: lines per block */
+    int32_t spot_b;      /* kind 0: threads per block; kind 1: segments per line */
+    int32_t var_kind;    /* 0: one shared tile per warp; 1: two tiles, copies pipelined */
+    int32_t var_warps;   /* warps per variance-solve block */
+    int32_t reserved[3];
+} fdadi_heston_plan_t;
+
 typedef struct fdadi_heston_batch {
     int32_t n_options;
     int32_t scheme;          /* FDADI_SCHEME_DOUGLAS or FDADI_SCHEME_HV (main segment) */
@@ -176,6 +187,7 @@ typedef struct fdadi_heston_batch {
     const double *params;    /* DEVICE [n_options][5]: r, kappa, theta, sigma, rho */
     const double *dt;        /* DEVICE [n_options] main-segment step */
     const int32_t *barrier;  /* DEVICE [n_options] nonzero: up-and-out (Dirichlet 0 at S_max), or NULL */
+    const fdadi_heston_plan_t *plan; /* HOST launch plan of the line solves, or NULL (heuristic) */
 } fdadi_heston_batch_t;
 
 /* drop the mixed operator of options with rho == 0, as the GPU reference
@@ -221,6 +233,18 @@ int64_t fdadi_heston_launch_count(const fdadi_heston_batch_t *batch);
 #define FDADI_STAGE_SPOT_SOLVE_IMPLICIT 8 /* W -> V (implicit plan) */
 int fdadi_heston_stage(const fdadi_heston_batch_t *batch, void *workspace,
                        int64_t workspace_bytes, double *V, int32_t stage, void *stream);
+
+/* Autotuner: time every launch plan variant of the spot and variance line
+ * solves on this prepared batch (reps launches each, in place on the stage
+ * buffer W, so the state V is untouched; W holds garbage afterwards, which
+ * every step overwrites) and write the fastest to *plan. Synchronises the
+ * stream. Pass the plan back in batch->plan for fdadi_heston_run. */
+int fdadi_heston_tune(const fdadi_heston_batch_t *batch, void *workspace,
+                      int64_t workspace_bytes, int32_t reps, fdadi_heston_plan_t *plan,
+                      void *stream);
+
+/* The plan fdadi_heston_run uses for this batch when batch->plan is NULL. */
+int fdadi_heston_default_plan(const fdadi_heston_batch_t *batch, fdadi_heston_plan_t *plan);
 
 /* FP64 throughput probe: a dependent-chain-free DFMA loop on every SM;
  * writes one value per thread to out (>= blocks*threads doubles) and returns

@@ -1,0 +1,174 @@
+"""Every launch plan of the batched engine's line solves against the oracle
+and the reference's golden outputs, and the autotuner.
+
+The partitioned spot solve and the pipelined variance solve reassociate the
+Thomas recurrences, so they are held to the spec bars (price within
+1e-10 relative, grid within 1e-9 of its max-norm), not bit equality.
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+pytestmark = pytest.mark.gpu
+
+from oracle import oracle as O  # noqa: E402
+
+HV_THETA = 0.5 + np.sqrt(3) / 6
+
+
+def _rel(a, b):
+    return np.abs(a - b).max() / np.abs(b).max()
+
+
+@pytest.fixture(scope="module")
+def cuda():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from fd_adi_gb300 import _lib
+    _lib.load()
+    return torch.device("cuda", 0)
+
+
+@pytest.fixture(scope="module")
+def uneven(cuda):
+    """Sixteen options, uneven grids (nS 32..96 so some lines are shorter than
+    a partitioned plan's segment count), with the oracle's solution.
+
+    Coarse grids with long HV steps can amplify rounding by 1e5: on some seeds
+    the oracle built with and without FMA contraction differs by 3e-10 in a
+    price, so no reordering of the arithmetic could meet a 1e-10 bar there.
+    This seed's batch is well conditioned (that spread is 5e-14 in price and
+    9e-13 of the grid's max), so the bars test the plans, not the seed."""
+    from fd_adi_gb300 import HestonOption, mesh
+    from fd_adi_gb300.batch import payoff_grids
+    rng = np.random.RandomState(21)
+    opts, meshes = [], []
+    for k in range(16):
+        K = 100 * rng.uniform(0.7, 1.3)
+        v0 = rng.uniform(0.01, 0.16)
+        o = HestonOption(spot=100., strike=K, interest_rate=rng.uniform(0, 0.08), variance=v0,
+                         tenor=rng.uniform(0.1, 2.0), mean_reversion=rng.uniform(0.5, 5),
+                         mean_variance=rng.uniform(0.01, 0.16), vol_of_variance=rng.uniform(0.1, 1),
+                         correlation=rng.uniform(-0.9, 0))
+        nS = int(rng.choice(np.arange(32, 97, 16)))
+        nv = int(rng.choice(np.arange(16, 81, 8)))
+        opts.append(o)
+        meshes.append(mesh.heston_meshes(100., K, v0, nS, nv, 8 * K, 5.0))
+    n = 20
+    dts = [o.tenor / n for o in opts]
+    V0 = payoff_grids(opts, meshes)
+    ref = O.heston_batch(meshes, [o.params() for o in opts], V0,
+                         [[("implicit", 2, dt / 2, 1.0), ("hv", n - 1, dt, HV_THETA)] for dt in dts])
+    kw = dict(scheme="hv", n_steps=n - 1, dt=dts, theta=HV_THETA, implicit_steps=2,
+              implicit_dt_factor=0.5)
+    return opts, meshes, V0, ref, kw
+
+
+def _check(out, opts, meshes, ref):
+    from fd_adi_gb300 import mesh as M
+    for k in range(len(opts)):
+        assert _rel(out[k], ref[k]) < 1e-9, k
+        i, j = M.price_index(meshes[k][0], meshes[k][1], 100., opts[k].variance.value)
+        assert abs(out[k][i, j] - ref[k][i, j]) <= 1e-10 * abs(ref[k][i, j]), k
+
+
+@pytest.mark.parametrize("k", range(16), ids=lambda k: "spot%d" % k)
+def test_spot_plan_vs_oracle(uneven, k):
+    from fd_adi_gb300.batch import HestonBatch, SPOT_PLANS, VAR_PLANS, make_plan
+    opts, meshes, V0, ref, kw = uneven
+    b = HestonBatch(opts, meshes, plan=make_plan(SPOT_PLANS[k], VAR_PLANS[0]), **kw)
+    assert b.plan == make_plan(SPOT_PLANS[k], VAR_PLANS[0])
+    _check(b.solve(V0), opts, meshes, ref)
+
+
+@pytest.mark.parametrize("k", range(5), ids=lambda k: "var%d" % k)
+def test_var_plan_vs_oracle(uneven, k):
+    from fd_adi_gb300.batch import HestonBatch, SPOT_PLANS, VAR_PLANS, make_plan
+    opts, meshes, V0, ref, kw = uneven
+    b = HestonBatch(opts, meshes, plan=make_plan(SPOT_PLANS[0], VAR_PLANS[k]), **kw)
+    _check(b.solve(V0), opts, meshes, ref)
+
+
+def test_plan_list_is_complete(cuda):
+    from fd_adi_gb300.batch import SPOT_PLANS, VAR_PLANS
+    assert len(SPOT_PLANS) == 16 and len(VAR_PLANS) == 5
+
+
+def test_unknown_plan_is_rejected(uneven):
+    from fd_adi_gb300.batch import HestonBatch
+    opts, meshes, V0, ref, kw = uneven
+    b = HestonBatch(opts[:2], meshes[:2], **dict(kw, dt=kw["dt"][:2]))
+    b.set_plan({"spot_kind": 1, "spot_a": 7, "spot_b": 3, "var_kind": 0, "var_warps": 4})
+    with pytest.raises(ValueError, match="plan"):
+        b.solve(V0[:2])
+
+
+@pytest.mark.parametrize("plan", [((1, 32, 32), (1, 4)), ((1, 8, 128), (1, 1)),
+                                  ((0, 8, 32), (1, 2))])
+def test_config1_golden_with_plan(cuda, golden, plan):
+    """Config 1 (150x150, 2 implicit half-steps + Douglas) against the
+    reference's golden output under partitioned and pipelined plans."""
+    from fd_adi_gb300.batch import HestonBatch, payoff_grids, make_plan
+    from fd_adi_gb300 import HestonOption
+    g = golden("config1")
+    opt = HestonOption(spot=100., strike=100., interest_rate=0.06, volatility=0.2, tenor=1.0,
+                       mean_reversion=1.0, mean_variance=0.04, vol_of_variance=0.2,
+                       correlation=0.0)
+    mesh = (g["S"], g["v"])
+    n, dt = 150, 1.0 / 150
+    b = HestonBatch([opt], [mesh], scheme="douglas", n_steps=n - 1, dt=dt, theta=0.5,
+                    implicit_steps=2, implicit_dt_factor=0.5, plan=make_plan(*plan))
+    V = b.solve(payoff_grids([opt], [mesh]))[0]
+    idx = tuple(g["idx"])
+    assert abs(V[idx] - g["price"]) <= 1e-10 * abs(g["price"])
+    assert np.abs(V - g["V"]).max() <= 1e-9 * np.abs(g["V"]).max()
+
+
+def test_config2_golden_partitioned(cuda, golden):
+    """1024x512 (long spot lines: the partitioned solve's case) against the
+    reference's golden output."""
+    from fd_adi_gb300.batch import HestonBatch, make_plan
+    g = golden("config2_short")
+    S, v = g["S"], g["v"]
+    V0 = np.maximum(S[:, None] - 100.0, 0) * np.ones((1, v.size))
+    b = HestonBatch([(0.06, 1.0, 0.04, 0.5, -0.7)], [(S, v)], scheme="hv", n_steps=3,
+                    dt=1.0 / 1000, theta=HV_THETA, implicit_steps=2, implicit_dt_factor=0.5,
+                    plan=make_plan((1, 8, 128), (1, 2)))
+    V = b.solve([V0])[0]
+    idx = tuple(g["idx"])
+    assert abs(V[idx] - g["price"]) <= 1e-10 * abs(g["price"])
+    assert np.abs(V[::16, ::8] - g["V_sub"]).max() <= 1e-9 * np.abs(g["V_sub"]).max()
+    assert abs(V.sum() - g["sum"]) <= 1e-10 * abs(g["sum"])
+
+
+def test_tune_keeps_state_and_picks_a_listed_plan(uneven, tmp_path, monkeypatch):
+    from fd_adi_gb300 import batch as B
+    opts, meshes, V0, ref, kw = uneven
+    monkeypatch.setenv("FDADI_TUNE_CACHE", str(tmp_path / "plans.json"))
+    b = B.HestonBatch(opts, meshes, **kw)
+    V = b.pack(V0)
+    before = V.clone()
+    plan = b.tune(reps=2, force=True)
+    torch.cuda.synchronize()
+    assert torch.equal(V, before)       # tuning touches the stage buffers only
+    assert (plan["spot_kind"], plan["spot_a"], plan["spot_b"]) in B.SPOT_PLANS
+    assert (plan["var_kind"], plan["var_warps"]) in B.VAR_PLANS
+    b.run(V)
+    _check(b.unpack(V), opts, meshes, ref)
+    # the plan is cached by shape, in the process and in the JSON file
+    assert (tmp_path / "plans.json").exists()
+    b2 = B.HestonBatch(opts, meshes, plan="auto", **kw)
+    assert b2.plan == plan
+
+
+def test_tuned_graph_run(uneven):
+    """A tuned plan inside the CUDA graph gives the direct run's result."""
+    from fd_adi_gb300.batch import HestonBatch
+    opts, meshes, V0, ref, kw = uneven
+    b = HestonBatch(opts, meshes, plan="auto", **kw)
+    direct = b.solve(V0)
+    gb = HestonBatch(opts, meshes, plan=b.plan, graph=True, **kw)
+    out = gb.solve(V0)
+    for k in range(len(opts)):
+        np.testing.assert_array_equal(out[k], direct[k])
