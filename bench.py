@@ -542,6 +542,8 @@ def main():
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--no-tune", action="store_true",
                     help="line-solve launch plan from the size heuristic, not the autotuner")
+    ap.add_argument("--plan", default=None,
+                    help="launch plan as JSON (fdadi_heston_plan_t fields) instead of tuning")
     ap.add_argument("--workload", default="batch", choices=["batch", "config2", "surrogate", "gemm"])
     ap.add_argument("--train", type=int, default=1 << 17)
     ap.add_argument("--test", type=int, default=1 << 13)
@@ -584,7 +586,8 @@ def main():
     t_tune = time.perf_counter()
     batch = HestonBatch(params, meshes, scheme="hv", n_steps=nt - 1, dt=dts, theta=HV_THETA,
                         implicit_steps=2, implicit_dt_factor=0.5, graph=True,
-                        plan=None if args.no_tune else "auto")
+                        plan=(json.loads(args.plan) if args.plan else
+                              None if args.no_tune else "auto"))
     t_tune = time.perf_counter() - t_tune
     # device-resident inputs (value) and pinned host copies (e2e)
     V0_dev = batch.pack(payoffs(w, meshes))
@@ -689,7 +692,7 @@ def main():
                              "peak_source": "measured live (fdadi_fp64_probe)",
                              "flops_per_point": STAGE_FLOPS[dom]},
                "stage_ms": {k: round(v[0], 4) for k, v in st.items()},
-               "plan": dict(batch.plan, tuned=not args.no_tune,
+               "plan": dict(batch.plan, tuned=not (args.no_tune or args.plan),
                             setup_s=round(t_tune, 2)),
                "clocks": clk}
         if args.cpu_sample > 0:

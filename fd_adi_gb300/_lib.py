@@ -45,16 +45,17 @@ class HestonPlan(ctypes.Structure):
     """fdadi_heston_plan_t"""
     _fields_ = [("spot_kind", ctypes.c_int32), ("spot_a", ctypes.c_int32),
                 ("spot_b", ctypes.c_int32), ("var_kind", ctypes.c_int32),
-                ("var_warps", ctypes.c_int32), ("reserved", ctypes.c_int32 * 3)]
+                ("var_warps", ctypes.c_int32), ("groups", ctypes.c_int32),
+                ("expl_per_sm", ctypes.c_int32), ("reserved", ctypes.c_int32 * 1)]
 
-    FIELDS = ("spot_kind", "spot_a", "spot_b", "var_kind", "var_warps")
+    FIELDS = ("spot_kind", "spot_a", "spot_b", "var_kind", "var_warps", "groups", "expl_per_sm")
 
     def as_dict(self):
         return {k: int(getattr(self, k)) for k in self.FIELDS}
 
     @classmethod
     def from_dict(cls, d):
-        return cls(*[int(d[k]) for k in cls.FIELDS])
+        return cls(*[int(d.get(k, 1 if k == "groups" else 0)) for k in cls.FIELDS])
 
 
 class HestonBatch(ctypes.Structure):

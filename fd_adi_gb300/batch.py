@@ -33,10 +33,13 @@ SPOT_PLANS = [(0, 1, 128), (0, 1, 64), (0, 1, 256), (0, 4, 32), (0, 8, 32), (0, 
 VAR_PLANS = [(0, 4), (0, 2), (1, 1), (1, 2), (1, 4)]
 
 
-def make_plan(spot, var):
-    """Plan dict from a SPOT_PLANS and a VAR_PLANS entry."""
+def make_plan(spot, var, groups=1, expl_per_sm=0):
+    """Plan dict from a SPOT_PLANS and a VAR_PLANS entry, a number of option
+    groups (1..4) whose explicit stages and line solves overlap, and the
+    explicit stage's blocks per SM (0: one block per tile)."""
     return {"spot_kind": spot[0], "spot_a": spot[1], "spot_b": spot[2],
-            "var_kind": var[0], "var_warps": var[1]}
+            "var_kind": var[0], "var_warps": var[1], "groups": groups,
+            "expl_per_sm": expl_per_sm}
 
 
 # Tuned launch plans by batch shape (this process); FDADI_TUNE_CACHE names a

@@ -168,7 +168,11 @@ typedef struct fdadi_heston_plan {
     int32_t spot_b;      /* kind 0: threads per block; kind 1: segments per line */
     int32_t var_kind;    /* 0: one shared tile per warp; 1: two tiles, copies pipelined */
     int32_t var_warps;   /* warps per variance-solve block */
-    int32_t reserved[3];
+    int32_t groups;      /* option groups whose explicit stages and solves overlap
+                          * (1..4; 0 counts as 1) */
+    int32_t expl_per_sm; /* explicit stage: 0 = one block per tile; n = n blocks per SM
+                          * looping over tiles (leaves room for another group's solves) */
+    int32_t reserved[1];
 } fdadi_heston_plan_t;
 
 typedef struct fdadi_heston_batch {
@@ -217,7 +221,8 @@ int fdadi_heston_run(const fdadi_heston_batch_t *batch, void *workspace,
 int fdadi_gather(const double *V, const int64_t *flat_index, double *out, int64_t n,
                  void *stream);
 
-/* Number of kernel launches fdadi_heston_run issues for this batch. */
+/* Number of kernel launches fdadi_heston_run issues for this batch (each
+ * stage is launched once per option group of the plan). */
 int64_t fdadi_heston_launch_count(const fdadi_heston_batch_t *batch);
 
 /* Launch one stage kernel of the time loop (for per-kernel timing; a run is
@@ -234,11 +239,14 @@ int64_t fdadi_heston_launch_count(const fdadi_heston_batch_t *batch);
 int fdadi_heston_stage(const fdadi_heston_batch_t *batch, void *workspace,
                        int64_t workspace_bytes, double *V, int32_t stage, void *stream);
 
-/* Autotuner: time every launch plan variant of the spot and variance line
- * solves on this prepared batch (reps launches each, in place on the stage
- * buffer W, so the state V is untouched; W holds garbage afterwards, which
- * every step overwrites) and write the fastest to *plan. Synchronises the
- * stream. Pass the plan back in batch->plan for fdadi_heston_run. */
+/* Autotuner: time every launch shape of the spot and variance line solves on
+ * this prepared batch (reps launches each, in place on the stage buffer W),
+ * then the number of option groups and the explicit stage's blocks per SM
+ * (two time steps per choice on a scratch state), and write the fastest plan
+ * to *plan. The state is untouched; the
+ * stage buffers hold garbage afterwards, which every step overwrites.
+ * Allocates the scratch state for the call and synchronises the stream. Pass
+ * the plan back in batch->plan for fdadi_heston_run. */
 int fdadi_heston_tune(const fdadi_heston_batch_t *batch, void *workspace,
                       int64_t workspace_bytes, int32_t reps, fdadi_heston_plan_t *plan,
                       void *stream);

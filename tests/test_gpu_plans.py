@@ -90,6 +90,33 @@ def test_var_plan_vs_oracle(uneven, k):
     _check(b.solve(V0), opts, meshes, ref)
 
 
+@pytest.mark.parametrize("groups,expl", [(2, 0), (3, 0), (4, 0), (1, 2), (2, 2), (4, 3)])
+@pytest.mark.parametrize("graph", [False, True])
+def test_option_groups_vs_oracle(uneven, groups, expl, graph):
+    """Option groups on side streams (direct) or graph branches: each group's
+    chain runs in order, explicit stages chained across groups; optionally
+    the explicit stage with a few blocks per SM looping over tiles."""
+    from fd_adi_gb300.batch import HestonBatch, SPOT_PLANS, VAR_PLANS, make_plan
+    opts, meshes, V0, ref, kw = uneven
+    plan = make_plan(SPOT_PLANS[0], VAR_PLANS[2], groups, expl)
+    b = HestonBatch(opts, meshes, plan=plan, graph=graph, **kw)
+    assert b.launches_per_run == groups * (3 * 2 + 6 * 19)
+    out = b.solve(V0)
+    _check(out, opts, meshes, ref)
+    one = HestonBatch(opts, meshes, plan=make_plan(SPOT_PLANS[0], VAR_PLANS[2], 1), **kw)
+    for k, x in enumerate(one.solve(V0)):
+        np.testing.assert_array_equal(out[k], x)   # same kernels per point: same bits
+
+
+def test_more_groups_than_options(uneven):
+    from fd_adi_gb300.batch import HestonBatch, SPOT_PLANS, VAR_PLANS, make_plan
+    opts, meshes, V0, ref, kw = uneven
+    b = HestonBatch(opts[:3], meshes[:3], plan=make_plan(SPOT_PLANS[0], VAR_PLANS[0], 4),
+                    **dict(kw, dt=kw["dt"][:3]))
+    assert b.launches_per_run == 3 * (3 * 2 + 6 * 19)
+    _check(b.solve(V0[:3]), opts[:3], meshes[:3], ref[:3])
+
+
 def test_plan_list_is_complete(cuda):
     from fd_adi_gb300.batch import SPOT_PLANS, VAR_PLANS
     assert len(SPOT_PLANS) == 16 and len(VAR_PLANS) == 5
@@ -154,6 +181,7 @@ def test_tune_keeps_state_and_picks_a_listed_plan(uneven, tmp_path, monkeypatch)
     assert torch.equal(V, before)       # tuning touches the stage buffers only
     assert (plan["spot_kind"], plan["spot_a"], plan["spot_b"]) in B.SPOT_PLANS
     assert (plan["var_kind"], plan["var_warps"]) in B.VAR_PLANS
+    assert 1 <= plan["groups"] <= 4
     b.run(V)
     _check(b.unpack(V), opts, meshes, ref)
     # the plan is cached by shape, in the process and in the JSON file
