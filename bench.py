@@ -47,9 +47,13 @@ STAGE_BYTES = {"explicit_hv0": 32, "explicit_hv3": 40, "spot_solve": 24, "var_so
 # 256-option cut of the batch workload (profiles/explicit_hv3_batch256.md);
 # traffic grows with the points processed, so a full launch is this x points.
 NCU_TRAFFIC_B_PER_POINT = {"explicit_hv3": 62.4}
-STAGE_FLOPS = {"explicit_hv0": 33.5, "explicit_hv3": 35.5, "spot_solve": 6, "var_solve_y2": 5,
-               "var_solve_v": 5, "explicit_implicit": 15.5, "var_solve_implicit": 5,
-               "spot_solve_implicit": 5}
+# FP64 pipe work per grid point: FP64 instructions x 2, so that a pipe fully
+# busy with DFMA (2 flops each; DMUL and DADD occupy it the same) reads as the
+# DFMA peak that fdadi_fp64_probe measures. The mixed-term row sums are formed
+# for 18 staged rows per 16-row tile: 3 x 18/16 = 3.375 instructions per point.
+STAGE_FLOPS = {"explicit_hv0": 30.75, "explicit_hv3": 28.75, "spot_solve": 8, "var_solve_y2": 6,
+               "var_solve_v": 6, "explicit_implicit": 12.75, "var_solve_implicit": 6,
+               "spot_solve_implicit": 6}
 
 
 def workload(n_options, seed, nt=200):
@@ -688,8 +692,8 @@ def main():
                             "bytes_per_point": STAGE_BYTES[dom],
                             "avg_launch_ms": avg_ms, "launches": st[dom][1]},
                "fp64_pipe": {"kernel": dom, "achieved": fp_ach, "peak": fp64,
-                             "unit": "TFLOP/s", "frac": fp_ach / fp64,
-                             "peak_source": "measured live (fdadi_fp64_probe)",
+                             "unit": "TFLOP/s (2 x FP64 instructions/s)", "frac": fp_ach / fp64,
+                             "peak_source": "measured live (fdadi_fp64_probe, DFMA only)",
                              "flops_per_point": STAGE_FLOPS[dom]},
                "stage_ms": {k: round(v[0], 4) for k, v in st.items()},
                "plan": dict(batch.plan, tuned=not (args.no_tune or args.plan),

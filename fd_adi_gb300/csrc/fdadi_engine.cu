@@ -87,6 +87,8 @@ struct Arena {
     double *dirS;              // [2 SV] Dirichlet values of the spot lines (low, high)
     // implicit plan (dt * factor, theta = 1, residual kept)
     double *w0i, *RSi, *LSi, *LVvi, *foldVi, *LVzi;
+    // HV corrector: (1/2 - theta) * F0 [3P] and w0 / 2 [3 SS]
+    double *F0h, *w0h;
     // stage buffers
     double *FV, *W, *T, *Y2;
     const double *theta;       // [n_opt]
@@ -200,6 +202,7 @@ struct BuildArgs {
     double dt_factor;  // implicit step = dt * dt_factor
     int smoothing;     // nonzero: build the implicit plan too
     int drop_zero_mixed;
+    int hv;            // nonzero: build the HV corrector's scaled copies too
 };
 
 __device__ __forceinline__ void opt_params(const BuildArgs &a, int o, double &r, double &kappa,
@@ -298,10 +301,16 @@ __global__ void build_points_kernel(Arena A, BuildArgs a) {
     const double dti = MUL(dt, a.dt_factor);
 
     const Row3 s = spot_row(S, n0, i, v[j], r, half_r, barrier);
+    double f0[3];
     if (s.dirichlet) {
-        A.F0[p] = 0.0; A.F0[P + p] = 1.0; A.F0[2 * P + p] = 0.0;
+        f0[0] = 0.0; f0[1] = 1.0; f0[2] = 0.0;
     } else {
-        A.F0[p] = MUL(s.sub, dt); A.F0[P + p] = MUL(s.mid, dt); A.F0[2 * P + p] = MUL(s.sup, dt);
+        f0[0] = MUL(s.sub, dt); f0[1] = MUL(s.mid, dt); f0[2] = MUL(s.sup, dt);
+    }
+    A.F0[p] = f0[0]; A.F0[P + p] = f0[1]; A.F0[2 * P + p] = f0[2];
+    if (a.hv) {
+        const double h = SUB(0.5, a.theta);
+        A.F0h[p] = MUL(f0[0], h); A.F0h[P + p] = MUL(f0[1], h); A.F0h[2 * P + p] = MUL(f0[2], h);
     }
     // mixed term rho sigma S_i v_j (D_S (x) D_v): the coefficient is
     // separable, so it is folded into the two stencils' weights
@@ -312,6 +321,10 @@ __global__ void build_points_kernel(Arena A, BuildArgs a) {
         const double cs = MUL(MUL(rho, sigma), S[i]);
         const double cm = MUL(cs, dt);
         A.w0[q] = sb * cm; A.w0[A.SS + q] = md * cm; A.w0[2 * A.SS + q] = sp * cm;
+        if (a.hv) {
+            A.w0h[q] = 0.5 * A.w0[q]; A.w0h[A.SS + q] = 0.5 * A.w0[A.SS + q];
+            A.w0h[2 * A.SS + q] = 0.5 * A.w0[2 * A.SS + q];
+        }
         if (a.smoothing) {
             const double ci = MUL(cs, dti);
             A.w0i[q] = sb * ci; A.w0i[A.SS + q] = md * ci; A.w0i[2 * A.SS + q] = sp * ci;
@@ -407,15 +420,50 @@ __device__ __forceinline__ void explicit_tile(const Arena &A, const double *__re
     const int64_t js = vo + j;
     const bool slow = fl & OPT_S_LOW_DIR, shigh = fl & OPT_S_HIGH_DIR;
 
-    double m = 0.0;
-    if (mixed && i > 0 && i < n0 - 1 && j > 0 && j < n1 - 1) {
-        const double *w0 = (MODE == ST_IMPLICIT) ? A.w0i : A.w0;
-        m = w0[so + i] * sT[ty][tx] + w0[A.SS + so + i] * sT[ty + 1][tx] +
-            w0[2 * A.SS + so + i] * sT[ty + 2][tx];
-    }
+    const bool mix_pt = mixed && i > 0 && i < n0 - 1 && j > 0 && j < n1 - 1;
     const double xc = sX[ty + 1][tx + 2];
-    if (MODE == ST_IMPLICIT) {
-        A.W[p] = xc + m;
+    if constexpr (MODE == ST_HV3) {
+        // Y0 - F(V - Y2)/2 - theta F0 Y2 = V + R + F(V)/2 + (1/2 - theta) F0 Y2
+        //   + F1 Y2 / 2 + M Y2 / 2, accumulated in one FMA chain with the
+        // (1/2 - theta) F0 and w0 / 2 copies built for this stage
+        double acc = V[p];
+        if (i == n0 - 1) acc += A.R0top[js];
+        acc = fma(0.5, A.FV[p], acc);
+        if ((i == 0 && slow) || (i == n0 - 1 && shigh)) {
+            acc = fma(0.5 - A.theta[o], i == 0 ? A.dirS[js] : A.dirS[A.SV + js], acc);
+        } else {
+            const double xm = (i == 1 && slow) ? A.dirS[js] : sX[ty][tx + 2];
+            const double xp = (i == n0 - 2 && shigh) ? A.dirS[A.SV + js] : sX[ty + 2][tx + 2];
+            acc = fma(A.F0h[p], xm, acc);
+            acc = fma(A.F0h[P + p], xc, acc);
+            acc = fma(A.F0h[2 * P + p], xp, acc);
+        }
+        if (mix_pt) {
+            acc = fma(A.w0h[so + i], sT[ty][tx], acc);
+            acc = fma(A.w0h[A.SS + so + i], sT[ty + 1][tx], acc);
+            acc = fma(A.w0h[2 * A.SS + so + i], sT[ty + 2][tx], acc);
+        }
+        double a1;
+        if (i == 0 && (fl & OPT_ROW0_ZERO)) {
+            a1 = A.F1z[o] * xc;
+        } else {
+            a1 = A.F1v[js] * sX[ty + 1][tx + 1] + A.F1v[A.SV + js] * xc +
+                 A.F1v[2 * A.SV + js] * sX[ty + 1][tx + 3];
+            if (j == n1 - 1) a1 += A.F1x[o] * sX[ty + 1][tx];
+        }
+        A.T[p] = a1;
+        A.W[p] = fma(0.5, a1, acc);
+        return;
+    }
+    if constexpr (MODE == ST_IMPLICIT) {
+        // x + M x, the mixed term chained onto x
+        double acc = xc;
+        if (mix_pt) {
+            acc = fma(A.w0i[so + i], sT[ty][tx], acc);
+            acc = fma(A.w0i[A.SS + so + i], sT[ty + 1][tx], acc);
+            acc = fma(A.w0i[2 * A.SS + so + i], sT[ty + 2][tx], acc);
+        }
+        A.W[p] = acc;
         return;
     }
     // spot operator with the Dirichlet rows forced (BandedOperator.pyx:339-344)
@@ -437,23 +485,20 @@ __device__ __forceinline__ void explicit_tile(const Arena &A, const double *__re
              A.F1v[2 * A.SV + js] * sX[ty + 1][tx + 3];
         if (j == n1 - 1) a1 += A.F1x[o] * sX[ty + 1][tx];
     }
-    const double theta = A.theta[o];
-    // T holds F1 x; the spot solve subtracts theta T from its result
-    if (MODE == ST_DOUGLAS || MODE == ST_HV0) {
-        // Y0 = V + F(V) + R; right-hand side of the spot solve Y0 - theta F0 V
-        const double fv = a0 + a1 + m;
-        if (MODE == ST_HV0) A.FV[p] = fv;
-        double base = xc + fv;
-        if (i == n0 - 1) base += A.R0top[js];
-        A.W[p] = fma(-theta, a0, base);
-        A.T[p] = a1;
-        return;
+    // F1 x + M x, the mixed term chained onto F1 x
+    double s = a1;
+    if (mix_pt) {
+        s = fma(A.w0[so + i], sT[ty][tx], s);
+        s = fma(A.w0[A.SS + so + i], sT[ty + 1][tx], s);
+        s = fma(A.w0[2 * A.SS + so + i], sT[ty + 2][tx], s);
     }
-    // ST_HV3: Y0 - F(V - Y2)/2 = V + R + (F V + F Y2)/2, minus theta F0 Y2
-    const double fy = a0 + a1 + m;
-    double vr = V[p];
-    if (i == n0 - 1) vr += A.R0top[js];
-    A.W[p] = fma(-theta, a0, fma(0.5, A.FV[p] + fy, vr));
+    // Y0 = V + F(V) + R; right-hand side of the spot solve Y0 - theta F0 V.
+    // T holds F1 x; the spot solve subtracts theta T from its result.
+    const double fv = s + a0;
+    if (MODE == ST_HV0) A.FV[p] = fv;
+    double base = xc + fv;
+    if (i == n0 - 1) base += A.R0top[js];
+    A.W[p] = fma(-A.theta[o], a0, base);
     A.T[p] = a1;
 }
 
@@ -461,7 +506,7 @@ __device__ __forceinline__ void explicit_tile(const Arena &A, const double *__re
 // fewer blocks) each block loops over tiles, so the stage can be held to a
 // share of every SM while line solves of another option group run beside it.
 template <int MODE>
-__global__ void __launch_bounds__(EXPL_THREADS) explicit_kernel(Arena A, const double *__restrict__ V,
+__global__ void __launch_bounds__(EXPL_THREADS, 4) explicit_kernel(Arena A, const double *__restrict__ V,
                                                                   int64_t tile0, int64_t tile1) {
     __shared__ double sX[XR][XCP];
     __shared__ double sT[XR][TJ];
@@ -924,7 +969,7 @@ struct Layout {
     int64_t o_F0, o_w0, o_w1, o_LS, o_R0top, o_F1v, o_F1x, o_F1z, o_LVv, o_foldV, o_LVz,
         o_dirS;
     int64_t o_w0i, o_RSi, o_LSi, o_LVvi, o_foldVi, o_LVzi;
-    int64_t o_FV, o_W, o_T, o_Y2;
+    int64_t o_FV, o_W, o_T, o_Y2, o_F0h, o_w0h;
     int64_t bytes = 0;
     std::vector<int64_t> p_off, s_off, v_off, tile_off, task_off;
 };
@@ -984,8 +1029,12 @@ static int make_layout(const fdadi_heston_batch_t *b, Layout &L) {
         L.o_w0i = L.o_RSi = L.o_LSi = L.o_LVvi = L.o_foldVi = L.o_LVzi = -1;
     }
     L.o_W = take(D * L.P); L.o_T = take(D * L.P);
-    if (L.hv) { L.o_FV = take(D * L.P); L.o_Y2 = take(D * L.P); }
-    else L.o_FV = L.o_Y2 = -1;
+    if (L.hv) {
+        L.o_FV = take(D * L.P); L.o_Y2 = take(D * L.P);
+        L.o_F0h = take(3 * D * L.P); L.o_w0h = take(3 * D * L.SS);
+    } else {
+        L.o_FV = L.o_Y2 = L.o_F0h = L.o_w0h = -1;
+    }
     L.bytes = off;
     return FDADI_OK;
 }
@@ -1009,6 +1058,7 @@ static Arena arena_view(const Layout &L, char *ws) {
     A.w0i = ptr(L.o_w0i); A.RSi = ptr(L.o_RSi); A.LSi = ptr(L.o_LSi); A.LVvi = ptr(L.o_LVvi);
     A.foldVi = ptr(L.o_foldVi); A.LVzi = ptr(L.o_LVzi);
     A.FV = ptr(L.o_FV); A.W = ptr(L.o_W); A.T = ptr(L.o_T); A.Y2 = ptr(L.o_Y2);
+    A.F0h = ptr(L.o_F0h); A.w0h = ptr(L.o_w0h);
     return A;
 }
 
@@ -1468,7 +1518,8 @@ int fdadi_heston_prepare(const fdadi_heston_batch_t *b, void *workspace, int64_t
     FDADI_CUDA(cudaMemcpyAsync(ws + L.o_theta, theta.data(), 8 * L.n_opt, cudaMemcpyHostToDevice, st));
     Arena A = arena_view(L, ws);
     BuildArgs a{b->spots, b->vars, b->params, b->dt, b->barrier, b->theta, b->implicit_dt_factor,
-                L.smoothing ? 1 : 0, (b->flags & FDADI_HESTON_DROP_ZERO_MIXED) ? 1 : 0};
+                L.smoothing ? 1 : 0, (b->flags & FDADI_HESTON_DROP_ZERO_MIXED) ? 1 : 0,
+                L.hv ? 1 : 0};
     build_options_kernel<<<(unsigned)((L.n_opt + 127) / 128), 128, 0, st>>>(A, a);
     FDADI_CHECK_LAUNCH();
     build_points_kernel<<<(unsigned)L.n_tiles, EXPL_THREADS, 0, st>>>(A, a);
