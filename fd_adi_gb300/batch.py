@@ -26,11 +26,14 @@ HV_THETA = 0.5 + np.sqrt(3.0) / 6.0
 # Launch shapes the engine implements (fdadi_heston_plan_t fields): spot solve
 # (kind 0: line per thread, rows prefetched, threads per block; kind 1:
 # partitioned lines, lines per block, segments per line) and variance solve
-# (kind 0: one tile per warp; kind 1: two tiles, pipelined copies; warps per block).
+# (kind 0: one tile per warp, factors loaded in the recurrence; kind 1: two
+# tiles, pipelined copies, factors by shuffle; kind 2: one tile, factors by
+# shuffle; warps per block).
 SPOT_PLANS = [(0, 1, 128), (0, 1, 64), (0, 1, 256), (0, 4, 32), (0, 8, 32), (0, 8, 64),
               (1, 32, 4), (1, 32, 8), (1, 32, 16), (1, 32, 32), (1, 16, 16), (1, 16, 32),
-              (1, 16, 64), (1, 8, 32), (1, 8, 64), (1, 8, 128)]
-VAR_PLANS = [(0, 4), (0, 2), (1, 1), (1, 2), (1, 4)]
+              (1, 16, 64), (1, 8, 32), (1, 8, 64), (1, 8, 128), (0, 2, 64), (0, 2, 128),
+              (0, 4, 64), (0, 4, 128)]
+VAR_PLANS = [(0, 4), (0, 2), (1, 1), (1, 2), (1, 4), (2, 1), (2, 2), (2, 4)]
 
 
 def make_plan(spot, var, groups=1, expl_per_sm=0):

@@ -819,23 +819,25 @@ __device__ __forceinline__ void cp_async8(void *sdst, const void *gsrc) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(s), "l"(gsrc));
 }
 
-// Variance-line solve, pipelined: as var_solve_kernel (one warp per task of up
-// to 32 grid rows, 32x32 chunks through a padded shared tile), with two tiles
-// per warp so the cp.async copies of the next chunk are in flight while the
-// lanes run the current chunk's recurrence, and each chunk's Thomas factors
-// held one per lane and broadcast by shuffle (no global load on the
-// recurrence's path). The back substitution starts from the forward sweep's
-// last chunk, still in shared memory. Dynamic shared memory:
-// NW * 2 * 32 * VS_PITCH doubles.
-template <bool IMPLICIT, int NW>
+// Variance-line solve with the Thomas factors in registers: as
+// var_solve_kernel (one warp per task of up to 32 grid rows, 32x32 chunks
+// through a padded shared tile), with each chunk's factors held one per lane
+// and broadcast by shuffle, so no global load sits on the recurrence's path.
+// DB: two tiles per warp, the cp.async copies of the next chunk in flight
+// while the lanes run the current chunk; without DB one tile (half the shared
+// memory, twice the resident warps). The back substitution starts from the
+// forward sweep's last chunk, still in shared memory. Dynamic shared memory:
+// NW * (DB ? 2 : 1) * 32 * VS_PITCH doubles.
+template <bool IMPLICIT, int NW, bool DB>
 __global__ void __launch_bounds__(NW * 32) var_solve_pipe_kernel(Arena A, Span tasks,
                                                                  const double *src, double *dst) {
+    constexpr int NB = DB ? 2 : 1;
     extern __shared__ double vsm[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t task = tasks.lo + (int64_t)blockIdx.x * NW + warp;
     if (task >= tasks.hi) return;
     double(*tl)[32][VS_PITCH] =
-        reinterpret_cast<double(*)[32][VS_PITCH]>(vsm + (size_t)warp * 2 * 32 * VS_PITCH);
+        reinterpret_cast<double(*)[32][VS_PITCH]>(vsm + (size_t)warp * NB * 32 * VS_PITCH);
     const int4 tk = A.vtasks[task];
     const int o = tk.x, i0 = tk.y, rows = tk.z;
     const int n1 = A.n1[o];
@@ -860,16 +862,15 @@ __global__ void __launch_bounds__(NW * 32) var_solve_pipe_kernel(Arena A, Span t
     if (lane < min(32, n1)) { fa = L[vo + lane]; fi = L[SV + vo + lane]; }
     double dp = 0.0, rprev = 0.0;
     for (int ch = 0; ch < nch; ++ch) {
-        const int buf = ch & 1, c0 = ch << 5, w = min(32, n1 - c0);
+        const int buf = DB ? (ch & 1) : 0, c0 = ch << 5, w = min(32, n1 - c0);
         double na = 0.0, ni = 0.0;
         if (ch + 1 < nch) {
-            issue(src, ch + 1, buf ^ 1);
             const int c1 = c0 + 32;
+            if (DB) issue(src, ch + 1, buf ^ 1);
             if (lane < min(32, n1 - c1)) { na = L[vo + c1 + lane]; ni = L[SV + vo + c1 + lane]; }
-            asm volatile("cp.async.wait_group 1;");
-        } else {
-            asm volatile("cp.async.wait_group 0;");
         }
+        if (DB && ch + 1 < nch) asm volatile("cp.async.wait_group 1;");
+        else asm volatile("cp.async.wait_group 0;");
         __syncwarp();
         for (int c = 0; c < w; ++c) {
             const double ac = __shfl_sync(FULL, fa, c), ic = __shfl_sync(FULL, fi, c);
@@ -894,10 +895,12 @@ __global__ void __launch_bounds__(NW * 32) var_solve_pipe_kernel(Arena A, Span t
         __syncwarp();
         fa = na;
         fi = ni;
+        if (!DB && ch + 1 < nch) issue(src, ch + 1, 0);
     }
     // the next copies read dst back: order this lane's stores before them
     __threadfence_block();
-    // back substitution, last chunk first (already in buf (nch-1) & 1)
+    // back substitution, last chunk first (its forward results are still in
+    // the tile the forward sweep ended on)
     double fc = 0.0;
     {
         const int c0 = (nch - 1) << 5;
@@ -905,15 +908,14 @@ __global__ void __launch_bounds__(NW * 32) var_solve_pipe_kernel(Arena A, Span t
     }
     double x = 0.0;
     for (int ch = nch - 1; ch >= 0; --ch) {
-        const int buf = ch & 1, c0 = ch << 5, w = min(32, n1 - c0);
+        const int buf = DB ? (ch & 1) : 0, c0 = ch << 5, w = min(32, n1 - c0);
         double nc = 0.0;
         if (ch > 0) {
-            issue(dst, ch - 1, buf ^ 1);
+            if (DB) issue(dst, ch - 1, buf ^ 1);
             nc = L[2 * SV + vo + c0 - 32 + lane];
-            asm volatile("cp.async.wait_group 1;");
-        } else {
-            asm volatile("cp.async.wait_group 0;");
         }
+        if (DB && ch > 0) asm volatile("cp.async.wait_group 1;");
+        else asm volatile("cp.async.wait_group 0;");
         __syncwarp();
         for (int c = w - 1; c >= 0; --c) {
             const double cc = __shfl_sync(FULL, fc, c);
@@ -930,6 +932,7 @@ __global__ void __launch_bounds__(NW * 32) var_solve_pipe_kernel(Arena A, Span t
                 dst[base + (int64_t)rr * n1 + c0 + lane] = tl[buf][rr][lane];
         __syncwarp();
         fc = nc;
+        if (!DB && ch > 0) issue(dst, ch - 1, 0);
     }
 }
 
@@ -1106,19 +1109,20 @@ static const SpotVariant SPOT_VARIANTS[] = {
     SPOT_T(1, 128), SPOT_T(1, 64),  SPOT_T(1, 256), SPOT_T(4, 32),  SPOT_T(8, 32),
     SPOT_T(8, 64),  SPOT_S(32, 4),  SPOT_S(32, 8),  SPOT_S(32, 16), SPOT_S(32, 32),
     SPOT_S(16, 16), SPOT_S(16, 32), SPOT_S(16, 64), SPOT_S(8, 32),  SPOT_S(8, 64),
-    SPOT_S(8, 128)};
+    SPOT_S(8, 128), SPOT_T(2, 64),  SPOT_T(2, 128), SPOT_T(4, 64),  SPOT_T(4, 128)};
 #undef SPOT_T
 #undef SPOT_S
 
-constexpr int VAR_PIPE_SMEM_PER_WARP = 2 * 32 * VS_PITCH * (int)sizeof(double);
+constexpr int VAR_TILE_BYTES = 32 * VS_PITCH * (int)sizeof(double);
+#define VAR_P(NW, DB)                                                                   \
+    VarVariant{DB ? 1 : 2, NW, NW * (DB ? 2 : 1) * VAR_TILE_BYTES,                     \
+               var_solve_pipe_kernel<false, NW, DB>, var_solve_pipe_kernel<true, NW, DB>}
 static const VarVariant VAR_VARIANTS[] = {
     {0, 4, 0, var_solve_kernel<false, 4>, var_solve_kernel<true, 4>},
     {0, 2, 0, var_solve_kernel<false, 2>, var_solve_kernel<true, 2>},
-    {1, 1, VAR_PIPE_SMEM_PER_WARP, var_solve_pipe_kernel<false, 1>, var_solve_pipe_kernel<true, 1>},
-    {1, 2, 2 * VAR_PIPE_SMEM_PER_WARP, var_solve_pipe_kernel<false, 2>,
-     var_solve_pipe_kernel<true, 2>},
-    {1, 4, 4 * VAR_PIPE_SMEM_PER_WARP, var_solve_pipe_kernel<false, 4>,
-     var_solve_pipe_kernel<true, 4>}};
+    VAR_P(1, true), VAR_P(2, true), VAR_P(4, true),
+    VAR_P(1, false), VAR_P(2, false), VAR_P(4, false)};
+#undef VAR_P
 
 constexpr int N_SPOT_VARIANTS = sizeof(SPOT_VARIANTS) / sizeof(SPOT_VARIANTS[0]);
 constexpr int N_VAR_VARIANTS = sizeof(VAR_VARIANTS) / sizeof(VAR_VARIANTS[0]);

@@ -164,9 +164,10 @@ int fdadi_axpby(double *y, const double *x, double a, double b, int64_t n, void 
  * fdadi_heston_tune, or by a size heuristic when a batch has none). */
 typedef struct fdadi_heston_plan {
     int32_t spot_kind;   /* 0: one thread per spot line; 1: partitioned lines */
-    int32_t spot_a;      /* kind 0: rows prefetched ahead (1, 4 or 8); kind 1: lines per block */
+    int32_t spot_a;      /* kind 0: rows prefetched ahead (1, 2, 4 or 8); kind 1: lines per block */
     int32_t spot_b;      /* kind 0: threads per block; kind 1: segments per line */
-    int32_t var_kind;    /* 0: one shared tile per warp; 1: two tiles, copies pipelined */
+    int32_t var_kind;    /* 0: one shared tile per warp; 1: two tiles, copies pipelined,
+                          * factors by shuffle; 2: one tile, factors by shuffle */
     int32_t var_warps;   /* warps per variance-solve block */
     int32_t groups;      /* option groups whose explicit stages and solves overlap
                           * (1..4; 0 counts as 1) */

@@ -73,7 +73,7 @@ def _check(out, opts, meshes, ref):
         assert abs(out[k][i, j] - ref[k][i, j]) <= 1e-10 * abs(ref[k][i, j]), k
 
 
-@pytest.mark.parametrize("k", range(16), ids=lambda k: "spot%d" % k)
+@pytest.mark.parametrize("k", range(20), ids=lambda k: "spot%d" % k)
 def test_spot_plan_vs_oracle(uneven, k):
     from fd_adi_gb300.batch import HestonBatch, SPOT_PLANS, VAR_PLANS, make_plan
     opts, meshes, V0, ref, kw = uneven
@@ -82,7 +82,7 @@ def test_spot_plan_vs_oracle(uneven, k):
     _check(b.solve(V0), opts, meshes, ref)
 
 
-@pytest.mark.parametrize("k", range(5), ids=lambda k: "var%d" % k)
+@pytest.mark.parametrize("k", range(8), ids=lambda k: "var%d" % k)
 def test_var_plan_vs_oracle(uneven, k):
     from fd_adi_gb300.batch import HestonBatch, SPOT_PLANS, VAR_PLANS, make_plan
     opts, meshes, V0, ref, kw = uneven
@@ -119,7 +119,7 @@ def test_more_groups_than_options(uneven):
 
 def test_plan_list_is_complete(cuda):
     from fd_adi_gb300.batch import SPOT_PLANS, VAR_PLANS
-    assert len(SPOT_PLANS) == 16 and len(VAR_PLANS) == 5
+    assert len(SPOT_PLANS) == 20 and len(VAR_PLANS) == 8
 
 
 def test_unknown_plan_is_rejected(uneven):
