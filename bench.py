@@ -44,9 +44,9 @@ STAGE_BYTES = {"explicit_hv0": 32, "explicit_hv3": 40, "spot_solve": 24, "var_so
                "var_solve_v": 16, "explicit_implicit": 16, "var_solve_implicit": 16,
                "spot_solve_implicit": 16}
 # DRAM bytes per grid point per launch measured by ncu (--set full) on the
-# 256-option cut of the batch workload (profiles/explicit_hv3_batch256.md);
+# 256-option cut of the batch workload (profiles/explicit_hv_batch256.md);
 # traffic grows with the points processed, so a full launch is this x points.
-NCU_TRAFFIC_B_PER_POINT = {"explicit_hv3": 62.4}
+NCU_TRAFFIC_B_PER_POINT = {"explicit_hv0": 52.7, "explicit_hv3": 62.3}
 # FP64 pipe work per grid point: FP64 instructions x 2, so that a pipe fully
 # busy with DFMA (2 flops each; DMUL and DADD occupy it the same) reads as the
 # DFMA peak that fdadi_fp64_probe measures. The mixed-term row sums are formed
