@@ -80,7 +80,7 @@ class Gemm(ctypes.Structure):
                 ("out_f32", ctypes.c_void_p), ("ldo", ctypes.c_int64), ("strideO", ctypes.c_int64),
                 ("out_bf16", ctypes.c_void_p), ("ldh", ctypes.c_int64), ("strideH", ctypes.c_int64),
                 ("M", ctypes.c_int32), ("N", ctypes.c_int32), ("K", ctypes.c_int32),
-                ("act", ctypes.c_int32), ("problems", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("act", ctypes.c_int32), ("problems", ctypes.c_int32), ("variant", ctypes.c_int32),
                 ("status", ctypes.c_void_p)]
 
 

@@ -18,8 +18,12 @@
 // stage's mbarrier; every wait on an mbarrier is bounded and sets the status
 // word instead of hanging. The epilogue reads the accumulator rows with
 // tcgen05.ld (warp w owns TMEM lanes 32w..32w+31) and stores 16-byte vectors.
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <stdint.h>
+
+#include <algorithm>
+#include <mutex>
 
 #include "fdadi_internal.cuh"
 
@@ -244,6 +248,301 @@ __global__ void __launch_bounds__(GM_THREADS) umma_gemm_kernel(GemmArgs g) {
     }
 }
 
+// ---- warp-specialised persistent GEMM (TMA + tcgen05) ---------------------
+//
+// 576 threads per CTA, one CTA per SM, each looping over work units
+// (128-row tile, K split, problem):
+//   warp 0  (one lane) TMA producer: per 64-wide K chunk, one
+//           cp.async.bulk.tensor box of 8 K-elements x rows per K-slice of A
+//           and of B into a 4-stage shared-memory ring; a stage's mbarrier
+//           completes on the copies' transaction bytes;
+//   warp 1  allocates tensor memory (two N-column accumulators); one lane
+//           issues the tcgen05.mma of each staged chunk and commits them to the
+//           stage's "empty" barrier (freeing it for the producer) and, after a
+//           unit's last chunk, to the accumulator's "full" barrier;
+//   warps 2-17 epilogue: tcgen05.ld of the finished accumulator (warp w reads
+//           TMEM lanes 32 (w % 4) ..., and a quarter of the columns), bias /
+//           SiLU / SiLU'(aux), stores (or, with K split, fp32 atomic adds), then
+//           release the accumulator, so the epilogue of one unit overlaps the
+//           MMAs of the next; four warps per lane quarter hide the latency of
+//           the epilogue's loads, special functions and scattered row stores.
+// Shared-memory layout of a stage: K-slice c (8 elements) of the A tile at
+// c * 128 * 16 bytes, rows 16 bytes apart (what a TMA box {8, 128} writes),
+// i.e. the no-swizzle K-major core-matrix layout with K-adjacent core matrices
+// rows * 16 bytes apart (leading byte offset) and 8-row groups 128 bytes apart
+// (stride byte offset); the same for B with N rows. Every mbarrier wait is
+// bounded by clock; a timeout sets the status word and a shared abort flag
+// that every role polls, and the kernel drains its copies and MMAs before it
+// frees tensor memory and returns.
+constexpr int WS_STAGES = 4;
+constexpr int WS_EPI_WARPS = 16;                  // 4 per TMEM lane quarter
+constexpr int WS_THREADS = 64 + 32 * WS_EPI_WARPS;
+constexpr int WS_A_BYTES = GM_BM * GM_BK * 2;     // 16 KB
+constexpr int WS_B_BYTES = 256 * GM_BK * 2;       // 32 KB
+constexpr int WS_STAGE_BYTES = WS_A_BYTES + WS_B_BYTES;
+constexpr int WS_SMEM = WS_STAGES * WS_STAGE_BYTES + 1024;  // + barriers
+
+struct WsArgs {
+    GemmArgs g;
+    int m_tiles, ksplit, problems;
+    int k_per_split;         // multiple of 64
+    int a_shared, b_shared;  // operand shared by every problem (stride 0)
+};
+
+// Bounded wait that gives up when another role has aborted.
+__device__ __forceinline__ bool ws_wait(uint64_t *mbar, uint32_t parity, volatile int *abort) {
+    const long long t0 = clock64();
+    uint32_t done = 0;
+    while (!done) {
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+            "selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done) : "r"(smem_addr(mbar)), "r"(parity) : "memory");
+        if (done) break;
+        if (*abort) return false;
+        if (clock64() - t0 > GM_WAIT_CYCLES) {
+            *abort = 1;
+            return false;
+        }
+    }
+    return true;
+}
+
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *map, int x, int y,
+                                            int z, uint64_t *mbar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+        "[%0], [%1, {%2, %3, %4}], [%5];"
+        ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z),
+          "r"(smem_addr(mbar))
+        : "memory");
+}
+
+__device__ __forceinline__ void tcgen05_commit(uint64_t *mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                 ::"r"(smem_addr(mbar)) : "memory");
+}
+
+__global__ void __launch_bounds__(WS_THREADS, 1)
+    umma_gemm_ws_kernel(const __grid_constant__ CUtensorMap tmA,
+                        const __grid_constant__ CUtensorMap tmB, WsArgs w) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    const GemmArgs &g = w.g;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + WS_STAGES * WS_STAGE_BYTES);
+    uint64_t *empty = full + WS_STAGES;
+    uint64_t *acc_full = empty + WS_STAGES;   // [2]
+    uint64_t *acc_empty = acc_full + 2;       // [2]
+    uint64_t *drain = acc_empty + 2;          // MMA completion on abort
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(drain + 1);
+    volatile int *abort = reinterpret_cast<volatile int *>(tslot + 1);
+    const uint32_t sbase = smem_addr(smem);
+    const int N = g.N, K = g.K;
+    const uint32_t ncols = 2 * N <= 32 ? 32 : 2 * N <= 64 ? 64 : 2 * N <= 128 ? 128
+                         : 2 * N <= 256 ? 256 : 512;
+    const int units = w.m_tiles * w.ksplit * w.problems;
+
+    if (tid == 0) {
+        for (int s = 0; s < WS_STAGES; ++s) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&full[s])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&empty[s])));
+        }
+        for (int a = 0; a < 2; ++a) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&acc_full[a])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;"
+                         ::"r"(smem_addr(&acc_empty[a])), "r"(WS_EPI_WARPS));
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(drain)));
+        *abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     ::"r"(smem_addr(tslot)), "r"(ncols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = *tslot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            // producer
+            asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmA)));
+            asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmB)));
+            uint32_t it = 0;
+            bool ok = true;
+            for (int u = blockIdx.x; u < units && ok; u += gridDim.x) {
+                const int mt = u % w.m_tiles, ks = (u / w.m_tiles) % w.ksplit;
+                const int p = u / (w.m_tiles * w.ksplit);
+                const int k_lo = ks * w.k_per_split, k_hi = min(K, k_lo + w.k_per_split);
+                for (int k0 = k_lo; k0 < k_hi; k0 += GM_BK, ++it) {
+                    const int s = it % WS_STAGES;
+                    const uint32_t n = it / WS_STAGES;
+                    if (n > 0 && !ws_wait(&empty[s], (n - 1) & 1, abort)) { ok = false; break; }
+                    const int kc = min(GM_BK, k_hi - k0) >> 3;
+                    const uint32_t bytes = (uint32_t)kc * (GM_BM + N) * 16;
+                    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                                 ::"r"(smem_addr(&full[s])), "r"(bytes) : "memory");
+                    const uint32_t a0 = sbase + s * WS_STAGE_BYTES, b0 = a0 + WS_A_BYTES;
+                    for (int c = 0; c < kc; ++c) {
+                        tma_load_3d(a0 + c * GM_BM * 16, &tmA, k0 + 8 * c, mt * GM_BM,
+                                    w.a_shared ? 0 : p, &full[s]);
+                        tma_load_3d(b0 + c * N * 16, &tmB, k0 + 8 * c, 0, w.b_shared ? 0 : p,
+                                    &full[s]);
+                    }
+                }
+            }
+            // drain: every issued copy has landed and (normally) every stage
+            // has been released by the MMAs, so nothing arrives after exit
+            const uint32_t last = it;
+            for (uint32_t j = last > WS_STAGES ? last - WS_STAGES : 0; j < last; ++j) {
+                const int s = j % WS_STAGES;
+                const uint32_t n = j / WS_STAGES;
+                if (*abort) mbar_wait(&full[s], n & 1);   // copies in flight
+                else ws_wait(&empty[s], n & 1, abort);
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            // MMA issuer
+            const uint32_t idesc = umma_idesc(GM_BM, N);
+            uint32_t it = 0;
+            int lu = 0;
+            bool ok = true;
+            for (int u = blockIdx.x; u < units && ok; u += gridDim.x, ++lu) {
+                const int ks = (u / w.m_tiles) % w.ksplit;
+                const int k_lo = ks * w.k_per_split, k_hi = min(K, k_lo + w.k_per_split);
+                const int acc = lu & 1;
+                const uint32_t na = (uint32_t)(lu >> 1);
+                if (na > 0 && !ws_wait(&acc_empty[acc], (na - 1) & 1, abort)) { ok = false; break; }
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                const uint32_t d = tmem + (uint32_t)(acc * N);
+                bool first = true;
+                for (int k0 = k_lo; k0 < k_hi; k0 += GM_BK, ++it) {
+                    const int s = it % WS_STAGES;
+                    const uint32_t n = it / WS_STAGES;
+                    if (!ws_wait(&full[s], n & 1, abort)) { ok = false; break; }
+                    asm volatile("tcgen05.fence::after_thread_sync;");
+                    const int kw = min(GM_BK, k_hi - k0);
+                    const uint32_t a0 = sbase + s * WS_STAGE_BYTES, b0 = a0 + WS_A_BYTES;
+                    for (int q = 0; q < (kw >> 4); ++q) {
+                        const uint64_t ad = umma_desc(a0 + q * 2 * GM_BM * 16, GM_BM * 16, 128);
+                        const uint64_t bd = umma_desc(b0 + q * 2 * N * 16, N * 16, 128);
+                        const uint32_t accum = first ? 0u : 1u;
+                        first = false;
+                        asm volatile(
+                            "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+                            ::"r"(d), "l"(ad), "l"(bd), "r"(idesc), "r"(accum));
+                    }
+                    tcgen05_commit(&empty[s]);
+                }
+                if (!ok) break;
+                tcgen05_commit(&acc_full[acc]);
+            }
+            if (*abort) {
+                // let every issued MMA finish before tensor memory is freed
+                tcgen05_commit(drain);
+                mbar_wait(drain, 0);
+            }
+        }
+    } else {
+        // epilogue: warp w -> TMEM lane quarter w % 4, column part (w - 2) / 4
+        const int q = warp & 3, part = (warp - 2) >> 2;
+        const int nparts = N >= 128 ? 4 : N >= 64 ? 2 : 1;
+        const int cw = N / nparts;                 // 32, 64 or N (N <= 32)
+        const bool active = part < nparts;
+        const int row = q * 32 + lane;
+        int lu = 0;
+        for (int u = blockIdx.x; u < units; u += gridDim.x, ++lu) {
+            const int mt = u % w.m_tiles, p = u / (w.m_tiles * w.ksplit);
+            const int acc = lu & 1;
+            // lane 0 waits; the decision is warp-uniform (tcgen05.ld is .sync.aligned)
+            int ok = 1;
+            if (lane == 0) ok = ws_wait(&acc_full[acc], (uint32_t)(lu >> 1) & 1, abort) ? 1 : 0;
+            if (!__shfl_sync(0xffffffffu, ok, 0)) break;
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            if (active) {
+                const int m = mt * GM_BM + row;
+                const float *bias = g.bias ? g.bias + p * g.strideBias : nullptr;
+                const float *aux = g.aux ? g.aux + p * g.strideAux + (int64_t)m * g.ldaux : nullptr;
+                float *of = g.out_f32 ? g.out_f32 + p * g.strideO + (int64_t)m * g.ldo : nullptr;
+                bf16 *oh = g.out_bf16 ? g.out_bf16 + p * g.strideH + (int64_t)m * g.ldh : nullptr;
+                const int cend = part * cw + cw;
+                for (int c0 = part * cw; c0 < cend; c0 += 8) {
+                    uint32_t r[8];
+                    const uint32_t taddr =
+                        tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * N + c0);
+                    asm volatile(
+                        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+                          "=r"(r[6]), "=r"(r[7])
+                        : "r"(taddr));
+                    float b8[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+                    if (bias) {
+                        const float4 b0 = *reinterpret_cast<const float4 *>(bias + c0);
+                        const float4 b1 = *reinterpret_cast<const float4 *>(bias + c0 + 4);
+                        b8[0] = b0.x; b8[1] = b0.y; b8[2] = b0.z; b8[3] = b0.w;
+                        b8[4] = b1.x; b8[5] = b1.y; b8[6] = b1.z; b8[7] = b1.w;
+                    }
+                    float a8[8];
+                    if (g.act == 2) {
+                        const float4 a0 = *reinterpret_cast<const float4 *>(aux + c0);
+                        const float4 a1 = *reinterpret_cast<const float4 *>(aux + c0 + 4);
+                        a8[0] = a0.x; a8[1] = a0.y; a8[2] = a0.z; a8[3] = a0.w;
+                        a8[4] = a1.x; a8[5] = a1.y; a8[6] = a1.z; a8[7] = a1.w;
+                    }
+                    asm volatile("tcgen05.wait::ld.sync.aligned;");
+                    float x[8];
+#pragma unroll
+                    for (int e = 0; e < 8; ++e) x[e] = __uint_as_float(r[e]) + b8[e];
+                    if (w.ksplit > 1) {
+                        float4 *o4 = reinterpret_cast<float4 *>(of + c0);
+                        atomicAdd(o4, make_float4(x[0], x[1], x[2], x[3]));
+                        atomicAdd(o4 + 1, make_float4(x[4], x[5], x[6], x[7]));
+                        continue;
+                    }
+                    if (of) {
+                        float4 *o4 = reinterpret_cast<float4 *>(of + c0);
+                        o4[0] = make_float4(x[0], x[1], x[2], x[3]);
+                        o4[1] = make_float4(x[4], x[5], x[6], x[7]);
+                    }
+                    if (oh) {
+                        __align__(16) bf16 h[8];
+#pragma unroll
+                        for (int e = 0; e < 8; ++e) {
+                            float y = x[e];
+                            if (g.act == 1) {
+                                y = __fdividef(y, 1.0f + __expf(-y));
+                            } else if (g.act == 2) {
+                                const float sg = __fdividef(1.0f, 1.0f + __expf(-a8[e]));
+                                y *= sg * (1.0f + a8[e] * (1.0f - sg));
+                            }
+                            h[e] = __float2bfloat16(y);
+                        }
+                        *reinterpret_cast<uint4 *>(oh + c0) = *reinterpret_cast<const uint4 *>(h);
+                    }
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;");
+            __syncwarp();
+            if (lane == 0)
+                asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];"
+                             ::"r"(smem_addr(&acc_empty[acc])) : "memory");
+        }
+    }
+    __syncthreads();
+    if (*abort) {
+        if (tid == 0 && g.status) atomicExch(g.status, 1);
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols));
+    }
+}
+
 // out[c][r] = in[r][c] for an R x C bf16 matrix (per problem: blockIdx.z).
 __global__ void transpose_bf16_kernel(const bf16 *in, int64_t ldi, int64_t stride_in, bf16 *out,
                                       int64_t ldo, int64_t stride_out, int R, int C) {
@@ -388,6 +687,96 @@ using namespace fdadi;
 
 extern "C" {
 
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// cuTensorMapEncodeTiled from the driver (the library links the runtime only).
+static EncodeTiledFn encode_tiled() {
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                             &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    });
+    return fn;
+}
+
+// 3-D map {K, rows, problems} of a K-contiguous bf16 operand; one box is one
+// 8-element K-slice of box_rows rows (16 bytes per row).
+static int make_operand_map(CUtensorMap *m, const void *base, int64_t rows, int64_t K,
+                            int64_t ld, int64_t stride, int problems, int box_rows) {
+    EncodeTiledFn enc = encode_tiled();
+    FDADI_REQUIRE(enc != nullptr, "cuTensorMapEncodeTiled is not available from the driver");
+    const bool shared = stride == 0 || problems == 1;
+    cuuint64_t dims[3] = {(cuuint64_t)K, (cuuint64_t)rows, (cuuint64_t)(shared ? 1 : problems)};
+    cuuint64_t strides[2] = {(cuuint64_t)ld * 2,
+                             (cuuint64_t)(shared ? rows * ld : stride) * 2};
+    cuuint32_t box[3] = {8, (cuuint32_t)box_rows, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    const CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void *>(base), dims,
+                           strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                           CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    FDADI_REQUIRE(r == CUDA_SUCCESS, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return FDADI_OK;
+}
+
+static int launch_ws(const fdadi_gemm_t *a, const GemmArgs &g, cudaStream_t st) {
+    static bool attr[64] = {false};
+    int dev = 0;
+    FDADI_CUDA(cudaGetDevice(&dev));
+    FDADI_REQUIRE(dev >= 0 && dev < 64, "device ordinal out of range");
+    if (!attr[dev]) {
+        FDADI_CUDA(cudaFuncSetAttribute(umma_gemm_ws_kernel,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, WS_SMEM));
+        attr[dev] = true;
+    }
+    WsArgs w;
+    w.g = g;
+    w.problems = a->problems;
+    w.m_tiles = a->M / GM_BM;
+    w.a_shared = (a->strideA == 0 || a->problems == 1) ? 1 : 0;
+    w.b_shared = (a->strideB == 0 || a->problems == 1) ? 1 : 0;
+    // split K when there are too few output tiles to fill the GPU (the weight
+    // gradients: 2 tiles per member, K = batch); the splits add fp32 partial
+    // sums atomically into a zeroed output
+    const int sms = sm_count();
+    const int tiles = w.m_tiles * w.problems;
+    int ksplit = 1;
+    const bool plain = a->out_f32 && !a->out_bf16 && !a->bias && a->act == 0;
+    if (plain && tiles * 2 <= sms && a->K >= 4 * GM_BK) {
+        ksplit = std::min((sms + tiles - 1) / tiles, a->K / (2 * GM_BK));
+        ksplit = std::max(ksplit, 1);
+    }
+    int kps = (a->K + ksplit - 1) / ksplit;
+    kps = (kps + GM_BK - 1) / GM_BK * GM_BK;
+    ksplit = (a->K + kps - 1) / kps;
+    w.ksplit = ksplit;
+    w.k_per_split = kps;
+    if (ksplit > 1) {
+        for (int p = 0; p < a->problems; ++p)
+            FDADI_CUDA(cudaMemset2DAsync(a->out_f32 + (int64_t)p * a->strideO,
+                                         (size_t)a->ldo * sizeof(float), 0,
+                                         (size_t)a->N * sizeof(float), (size_t)a->M, st));
+    }
+    CUtensorMap mA, mB;
+    int rc = make_operand_map(&mA, a->A, a->M, a->K, a->lda, a->strideA, a->problems, GM_BM);
+    if (rc) return rc;
+    rc = make_operand_map(&mB, a->B, a->N, a->K, a->ldb, a->strideB, a->problems, a->N);
+    if (rc) return rc;
+    const int units = w.m_tiles * w.ksplit * w.problems;
+    const unsigned grid = (unsigned)std::min(units, sms);
+    umma_gemm_ws_kernel<<<grid, WS_THREADS, WS_SMEM, st>>>(mA, mB, w);
+    FDADI_CHECK_LAUNCH();
+    return FDADI_OK;
+}
+
 int fdadi_mlp_gemm(const fdadi_gemm_t *a, void *stream) {
     FDADI_REQUIRE(a && a->A && a->B, "null GEMM operand");
     FDADI_REQUIRE(a->M > 0 && a->M % 128 == 0, "GEMM M must be a positive multiple of 128 (%d)", a->M);
@@ -405,6 +794,11 @@ int fdadi_mlp_gemm(const fdadi_gemm_t *a, void *stream) {
     FDADI_REQUIRE(!a->out_bf16 || ((uintptr_t)a->out_bf16 % 16 == 0 && a->ldh % 8 == 0 &&
                                    a->strideH % 8 == 0 && a->ldh >= a->N),
                   "GEMM bf16 output must be 16-byte aligned with ldh, strideH multiples of 8");
+    FDADI_REQUIRE(!a->bias || ((uintptr_t)a->bias % 16 == 0 && a->strideBias % 4 == 0),
+                  "GEMM bias must be 16-byte aligned with strideBias a multiple of 4");
+    FDADI_REQUIRE(!a->aux || ((uintptr_t)a->aux % 16 == 0 && a->ldaux % 4 == 0 &&
+                              a->strideAux % 4 == 0),
+                  "GEMM aux must be 16-byte aligned with ldaux, strideAux multiples of 4");
     FDADI_REQUIRE(a->problems >= 1, "GEMM needs at least one problem");
     static bool attr[64] = {false};
     int dev = 0;
@@ -419,6 +813,8 @@ int fdadi_mlp_gemm(const fdadi_gemm_t *a, void *stream) {
                a->bias, a->strideBias, a->aux, a->ldaux, a->strideAux, a->out_f32, a->ldo,
                a->strideO, (bf16 *)a->out_bf16, a->ldh, a->strideH, a->M, a->N, a->K, a->act,
                a->status};
+    FDADI_REQUIRE(a->variant == 0 || a->variant == 1, "unknown GEMM variant %d", a->variant);
+    if (a->variant == 0) return launch_ws(a, g, as_stream(stream));
     dim3 grid(a->M / 128, a->problems);
     umma_gemm_kernel<<<grid, GM_THREADS, GM_SMEM, as_stream(stream)>>>(g);
     FDADI_CHECK_LAUNCH();

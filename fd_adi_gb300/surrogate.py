@@ -41,13 +41,13 @@ def _st():
 
 
 def gemm(A, lda, sA, B, ldb, sB, M, N, K, P, bias=None, sBias=0, aux=None, ldaux=0, sAux=0,
-         out_f32=None, ldo=0, sO=0, out_bf16=None, ldh=0, sH=0, act=0, status=None):
+         out_f32=None, ldo=0, sO=0, out_bf16=None, ldh=0, sH=0, act=0, status=None, variant=0):
     g = _lib.Gemm(A.data_ptr(), lda, sA, B.data_ptr(), ldb, sB,
                   bias.data_ptr() if bias is not None else None, sBias,
                   aux.data_ptr() if aux is not None else None, ldaux, sAux,
                   out_f32.data_ptr() if out_f32 is not None else None, ldo, sO,
                   out_bf16.data_ptr() if out_bf16 is not None else None, ldh, sH,
-                  M, N, K, act, P, 0, status.data_ptr() if status is not None else None)
+                  M, N, K, act, P, variant, status.data_ptr() if status is not None else None)
     _lib.call("fdadi_mlp_gemm", ctypes.byref(g), _st())
 
 

@@ -283,7 +283,11 @@ typedef struct fdadi_gemm {
     const float *aux; int64_t ldaux, strideAux;
     float *out_f32; int64_t ldo, strideO;
     void *out_bf16; int64_t ldh, strideH;
-    int32_t M, N, K, act, problems, reserved;
+    int32_t M, N, K, act, problems;
+    int32_t variant;   /* 0: persistent warp-specialised kernel (TMA producer warp, MMA warp,
+                        * epilogue warps, two tensor-memory accumulators; K split with fp32
+                        * atomic adds when there are few output tiles and no epilogue);
+                        * 1: one CTA per tile, two cp.async stages */
     int32_t *status;
 } fdadi_gemm_t;
 int fdadi_mlp_gemm(const fdadi_gemm_t *gemm, void *stream);
