@@ -315,24 +315,27 @@ def run_gemm(args):
     X = torch.zeros(M, 16)
     X[:, :8] = torch.rand(M, 8) * 2 - 1
     X = X.to(torch.bfloat16).to(dev)
-    for _ in range(args.warmup):
-        net.forward(X, M)
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(args.steps):
-        net.forward(X, M)
-    e1.record()
-    torch.cuda.synchronize()
-    net.check()
-    ms = e0.elapsed_time(e1) / args.steps
     flops = 2.0 * M * net.P * sum(k * n for k, n in LAYERS)
     with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
         peak = float(json.load(f).get("bf16_tflops", 1901.1))
-    ach = flops / (ms * 1e-3) / 1e12
-    print(json.dumps({"workload": "surrogate ensemble forward", "queries": M, "ms": ms,
-                      "queries_per_s": M / (ms * 1e-3), "tflops": ach, "peak": peak,
-                      "frac": ach / peak}))
+    out = {"workload": "surrogate ensemble forward", "queries": M, "peak": peak}
+    # inference (hidden pre-activations not stored) and the training forward
+    for name, keep in (("inference", False), ("training", True)):
+        for _ in range(args.warmup):
+            net.forward(X, M, keep_preact=keep)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            net.forward(X, M, keep_preact=keep)
+        e1.record()
+        torch.cuda.synchronize()
+        net.check()
+        ms = e0.elapsed_time(e1) / args.steps
+        ach = flops / (ms * 1e-3) / 1e12
+        out[name] = {"ms": ms, "queries_per_s": M / (ms * 1e-3), "tflops": ach,
+                     "frac": ach / peak}
+    print(json.dumps(out))
     return 0
 
 
@@ -397,11 +400,11 @@ def run_surrogate(args):
     Qd = torch.as_tensor(Q, device=dev)
     M = (nq // 128) * 128
     X, _, _ = sur.feat(Qd[:M].contiguous())
-    sur.net.forward(X, M)
+    sur.net.forward(X, M, keep_preact=False)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
     for _ in range(5):
-        sur.net.forward(X, M)
+        sur.net.forward(X, M, keep_preact=False)
     e1.record()
     torch.cuda.synchronize()
     fwd_ms = e0.elapsed_time(e1) / 5

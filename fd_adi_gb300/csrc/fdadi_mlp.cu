@@ -250,22 +250,25 @@ __global__ void __launch_bounds__(GM_THREADS) umma_gemm_kernel(GemmArgs g) {
 
 // ---- warp-specialised persistent GEMM (TMA + tcgen05) ---------------------
 //
-// 576 threads per CTA, one CTA per SM, each looping over work units
+// 320 threads per CTA, one CTA per SM, each looping over work units
 // (128-row tile, K split, problem):
 //   warp 0  (one lane) TMA producer: per 64-wide K chunk, one
 //           cp.async.bulk.tensor box of 8 K-elements x rows per K-slice of A
-//           and of B into a 4-stage shared-memory ring; a stage's mbarrier
+//           and of B into a 3-stage shared-memory ring; a stage's mbarrier
 //           completes on the copies' transaction bytes;
 //   warp 1  allocates tensor memory (two N-column accumulators); one lane
 //           issues the tcgen05.mma of each staged chunk and commits them to the
 //           stage's "empty" barrier (freeing it for the producer) and, after a
 //           unit's last chunk, to the accumulator's "full" barrier;
-//   warps 2-17 epilogue: tcgen05.ld of the finished accumulator (warp w reads
-//           TMEM lanes 32 (w % 4) ..., and a quarter of the columns), bias /
-//           SiLU / SiLU'(aux), stores (or, with K split, fp32 atomic adds), then
-//           release the accumulator, so the epilogue of one unit overlaps the
-//           MMAs of the next; four warps per lane quarter hide the latency of
-//           the epilogue's loads, special functions and scattered row stores.
+//   warps 2-9 epilogue: tcgen05.ld of the finished accumulator (warp w reads
+//           TMEM lanes 32 (w % 4) ..., and half of the columns), bias / SiLU /
+//           SiLU'(aux), then each 32-row x 32-column block is written to a
+//           swizzled shared-memory tile (conflict-free: the 16-byte granule
+//           index is XORed with the row, as the tensor map's swizzle mode
+//           expects) and one lane stores it with a TMA bulk tensor store, or,
+//           with K split, a TMA reduce-add of fp32 partial sums; the
+//           accumulator is released when it has been read, so the epilogue of
+//           one unit overlaps the MMAs of the next.
 // Shared-memory layout of a stage: K-slice c (8 elements) of the A tile at
 // c * 128 * 16 bytes, rows 16 bytes apart (what a TMA box {8, 128} writes),
 // i.e. the no-swizzle K-major core-matrix layout with K-adjacent core matrices
@@ -274,13 +277,17 @@ __global__ void __launch_bounds__(GM_THREADS) umma_gemm_kernel(GemmArgs g) {
 // bounded by clock; a timeout sets the status word and a shared abort flag
 // that every role polls, and the kernel drains its copies and MMAs before it
 // frees tensor memory and returns.
-constexpr int WS_STAGES = 4;
-constexpr int WS_EPI_WARPS = 16;                  // 4 per TMEM lane quarter
+constexpr int WS_STAGES = 3;
+constexpr int WS_EPI_WARPS = 8;                   // 2 per TMEM lane quarter
 constexpr int WS_THREADS = 64 + 32 * WS_EPI_WARPS;
 constexpr int WS_A_BYTES = GM_BM * GM_BK * 2;     // 16 KB
 constexpr int WS_B_BYTES = 256 * GM_BK * 2;       // 32 KB
 constexpr int WS_STAGE_BYTES = WS_A_BYTES + WS_B_BYTES;
-constexpr int WS_SMEM = WS_STAGES * WS_STAGE_BYTES + 1024;  // + barriers
+constexpr int WS_OUT_F32 = 32 * 32 * 4;           // staged 32x32 fp32 block
+constexpr int WS_OUT_BYTES = WS_OUT_F32 + 32 * 32 * 2;  // + its bf16 copy, per epilogue warp
+constexpr int WS_OUT_BASE = WS_STAGES * WS_STAGE_BYTES;
+constexpr int WS_BAR_BASE = WS_OUT_BASE + WS_EPI_WARPS * WS_OUT_BYTES;
+constexpr int WS_SMEM = WS_BAR_BASE + 1024;       // + barriers
 
 struct WsArgs {
     GemmArgs g;
@@ -325,11 +332,13 @@ __device__ __forceinline__ void tcgen05_commit(uint64_t *mbar) {
 
 __global__ void __launch_bounds__(WS_THREADS, 1)
     umma_gemm_ws_kernel(const __grid_constant__ CUtensorMap tmA,
-                        const __grid_constant__ CUtensorMap tmB, WsArgs w) {
+                        const __grid_constant__ CUtensorMap tmB,
+                        const __grid_constant__ CUtensorMap tmY,
+                        const __grid_constant__ CUtensorMap tmH, WsArgs w) {
     extern __shared__ __align__(1024) unsigned char smem[];
     const GemmArgs &g = w.g;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    uint64_t *full = reinterpret_cast<uint64_t *>(smem + WS_STAGES * WS_STAGE_BYTES);
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + WS_BAR_BASE);
     uint64_t *empty = full + WS_STAGES;
     uint64_t *acc_full = empty + WS_STAGES;   // [2]
     uint64_t *acc_empty = acc_full + 2;       // [2]
@@ -451,10 +460,15 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
     } else {
         // epilogue: warp w -> TMEM lane quarter w % 4, column part (w - 2) / 4
         const int q = warp & 3, part = (warp - 2) >> 2;
-        const int nparts = N >= 128 ? 4 : N >= 64 ? 2 : 1;
-        const int cw = N / nparts;                 // 32, 64 or N (N <= 32)
+        const int nparts = N >= 64 ? 2 : 1;
+        const int cw = N / nparts;                 // 16 .. 128 columns
+        const int bc = min(32, cw);                // columns per staged block
         const bool active = part < nparts;
         const int row = q * 32 + lane;
+        unsigned char *stage = smem + WS_OUT_BASE + (warp - 2) * WS_OUT_BYTES;
+        const uint32_t sy = smem_addr(stage), sh = sy + WS_OUT_F32;
+        const int ry = bc * 4, rh = bc * 2;        // staged row bytes (32, 64 or 128)
+        const bool has_y = g.out_f32 != nullptr, has_h = g.out_bf16 != nullptr;
         int lu = 0;
         for (int u = blockIdx.x; u < units; u += gridDim.x, ++lu) {
             const int mt = u % w.m_tiles, p = u / (w.m_tiles * w.ksplit);
@@ -468,11 +482,9 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
                 const int m = mt * GM_BM + row;
                 const float *bias = g.bias ? g.bias + p * g.strideBias : nullptr;
                 const float *aux = g.aux ? g.aux + p * g.strideAux + (int64_t)m * g.ldaux : nullptr;
-                float *of = g.out_f32 ? g.out_f32 + p * g.strideO + (int64_t)m * g.ldo : nullptr;
-                bf16 *oh = g.out_bf16 ? g.out_bf16 + p * g.strideH + (int64_t)m * g.ldh : nullptr;
                 const int cend = part * cw + cw;
-                for (int c0 = part * cw; c0 < cend; c0 += 8) {
-                    uint32_t r[8];
+                for (int c0 = part * cw; c0 < cend; c0 += bc) {
+                    uint32_t r[32];
                     const uint32_t taddr =
                         tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * N + c0);
                     asm volatile(
@@ -480,49 +492,105 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
                         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
                           "=r"(r[6]), "=r"(r[7])
                         : "r"(taddr));
-                    float b8[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-                    if (bias) {
-                        const float4 b0 = *reinterpret_cast<const float4 *>(bias + c0);
-                        const float4 b1 = *reinterpret_cast<const float4 *>(bias + c0 + 4);
-                        b8[0] = b0.x; b8[1] = b0.y; b8[2] = b0.z; b8[3] = b0.w;
-                        b8[4] = b1.x; b8[5] = b1.y; b8[6] = b1.z; b8[7] = b1.w;
-                    }
-                    float a8[8];
-                    if (g.act == 2) {
-                        const float4 a0 = *reinterpret_cast<const float4 *>(aux + c0);
-                        const float4 a1 = *reinterpret_cast<const float4 *>(aux + c0 + 4);
-                        a8[0] = a0.x; a8[1] = a0.y; a8[2] = a0.z; a8[3] = a0.w;
-                        a8[4] = a1.x; a8[5] = a1.y; a8[6] = a1.z; a8[7] = a1.w;
+                    asm volatile(
+                        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                        : "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+                          "=r"(r[14]), "=r"(r[15])
+                        : "r"(taddr + 8));
+                    if (bc == 32) {
+                        asm volatile(
+                            "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                            : "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]),
+                              "=r"(r[21]), "=r"(r[22]), "=r"(r[23])
+                            : "r"(taddr + 16));
+                        asm volatile(
+                            "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                            : "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
+                              "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+                            : "r"(taddr + 24));
                     }
                     asm volatile("tcgen05.wait::ld.sync.aligned;");
-                    float x[8];
+                    // the previous block's TMA stores must have read the staging tile
+                    if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+                    __syncwarp();
+                    for (int g8 = 0; g8 < bc; g8 += 8) {
+                        float x[8];
+                        if (bias) {
+                            const float4 b0 = *reinterpret_cast<const float4 *>(bias + c0 + g8);
+                            const float4 b1 = *reinterpret_cast<const float4 *>(bias + c0 + g8 + 4);
+                            x[0] = b0.x; x[1] = b0.y; x[2] = b0.z; x[3] = b0.w;
+                            x[4] = b1.x; x[5] = b1.y; x[6] = b1.z; x[7] = b1.w;
+                        } else {
 #pragma unroll
-                    for (int e = 0; e < 8; ++e) x[e] = __uint_as_float(r[e]) + b8[e];
-                    if (w.ksplit > 1) {
-                        float4 *o4 = reinterpret_cast<float4 *>(of + c0);
-                        atomicAdd(o4, make_float4(x[0], x[1], x[2], x[3]));
-                        atomicAdd(o4 + 1, make_float4(x[4], x[5], x[6], x[7]));
-                        continue;
-                    }
-                    if (of) {
-                        float4 *o4 = reinterpret_cast<float4 *>(of + c0);
-                        o4[0] = make_float4(x[0], x[1], x[2], x[3]);
-                        o4[1] = make_float4(x[4], x[5], x[6], x[7]);
-                    }
-                    if (oh) {
-                        __align__(16) bf16 h[8];
-#pragma unroll
-                        for (int e = 0; e < 8; ++e) {
-                            float y = x[e];
-                            if (g.act == 1) {
-                                y = __fdividef(y, 1.0f + __expf(-y));
-                            } else if (g.act == 2) {
-                                const float sg = __fdividef(1.0f, 1.0f + __expf(-a8[e]));
-                                y *= sg * (1.0f + a8[e] * (1.0f - sg));
-                            }
-                            h[e] = __float2bfloat16(y);
+                            for (int e = 0; e < 8; ++e) x[e] = 0.0f;
                         }
-                        *reinterpret_cast<uint4 *>(oh + c0) = *reinterpret_cast<const uint4 *>(h);
+#pragma unroll
+                        for (int e = 0; e < 8; ++e) x[e] += __uint_as_float(r[g8 + e]);
+                        if (has_y) {
+                            // 16-byte granules j = g8/4, g8/4 + 1 of row `lane`, swizzled
+#pragma unroll
+                            for (int hh = 0; hh < 2; ++hh) {
+                                const uint32_t lo = (uint32_t)(lane * ry + (g8 / 4 + hh) * 16);
+                                const uint32_t ph = lo ^ (((lo >> 7) & (uint32_t)(ry / 16 - 1)) << 4);
+                                asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};"
+                                             ::"r"(sy + ph), "f"(x[4 * hh]), "f"(x[4 * hh + 1]),
+                                               "f"(x[4 * hh + 2]), "f"(x[4 * hh + 3]) : "memory");
+                            }
+                        }
+                        if (has_h) {
+                            float a8[8];
+                            if (g.act == 2) {
+                                const float4 a0 = *reinterpret_cast<const float4 *>(aux + c0 + g8);
+                                const float4 a1 = *reinterpret_cast<const float4 *>(aux + c0 + g8 + 4);
+                                a8[0] = a0.x; a8[1] = a0.y; a8[2] = a0.z; a8[3] = a0.w;
+                                a8[4] = a1.x; a8[5] = a1.y; a8[6] = a1.z; a8[7] = a1.w;
+                            }
+                            __align__(16) bf16 h[8];
+#pragma unroll
+                            for (int e = 0; e < 8; ++e) {
+                                float y = x[e];
+                                if (g.act == 1) {
+                                    y = __fdividef(y, 1.0f + __expf(-y));
+                                } else if (g.act == 2) {
+                                    const float sg = __fdividef(1.0f, 1.0f + __expf(-a8[e]));
+                                    y *= sg * (1.0f + a8[e] * (1.0f - sg));
+                                }
+                                h[e] = __float2bfloat16(y);
+                            }
+                            const uint4 hv = *reinterpret_cast<const uint4 *>(h);
+                            const uint32_t lo = (uint32_t)(lane * rh + (g8 / 8) * 16);
+                            const uint32_t ph = lo ^ (((lo >> 7) & (uint32_t)(rh / 16 - 1)) << 4);
+                            asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};"
+                                         ::"r"(sh + ph), "r"(hv.x), "r"(hv.y), "r"(hv.z), "r"(hv.w)
+                                         : "memory");
+                        }
+                    }
+                    // make the staged tiles visible to the TMA (async proxy)
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    __syncwarp();
+                    if (lane == 0) {
+                        const int y0 = mt * GM_BM + q * 32;
+                        if (has_y) {
+                            if (w.ksplit > 1)
+                                asm volatile(
+                                    "cp.reduce.async.bulk.tensor.3d.global.shared::cta.add.tile.bulk_group "
+                                    "[%0, {%1, %2, %3}], [%4];"
+                                    ::"l"(reinterpret_cast<uint64_t>(&tmY)), "r"(c0), "r"(y0), "r"(p),
+                                      "r"(sy) : "memory");
+                            else
+                                asm volatile(
+                                    "cp.async.bulk.tensor.3d.global.shared::cta.tile.bulk_group "
+                                    "[%0, {%1, %2, %3}], [%4];"
+                                    ::"l"(reinterpret_cast<uint64_t>(&tmY)), "r"(c0), "r"(y0), "r"(p),
+                                      "r"(sy) : "memory");
+                        }
+                        if (has_h)
+                            asm volatile(
+                                "cp.async.bulk.tensor.3d.global.shared::cta.tile.bulk_group "
+                                "[%0, {%1, %2, %3}], [%4];"
+                                ::"l"(reinterpret_cast<uint64_t>(&tmH)), "r"(c0), "r"(y0), "r"(p),
+                                  "r"(sh) : "memory");
+                        asm volatile("cp.async.bulk.commit_group;" ::: "memory");
                     }
                 }
             }
@@ -532,6 +600,8 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
                 asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];"
                              ::"r"(smem_addr(&acc_empty[acc])) : "memory");
         }
+        // the stores are complete before the kernel ends
+        if (lane == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
     }
     __syncthreads();
     if (*abort) {
@@ -727,6 +797,31 @@ static int make_operand_map(CUtensorMap *m, const void *base, int64_t rows, int6
     return FDADI_OK;
 }
 
+// 3-D map {N, M, problems} of an output (fp32 or bf16, row-major with leading
+// dimension ld); one box is a 32-row x bc-column block, swizzled in shared
+// memory by its row size (bc * element bytes: 32, 64 or 128).
+static int make_output_map(CUtensorMap *m, void *base, CUtensorMapDataType type, int esize,
+                           int64_t M, int64_t N, int64_t ld, int64_t stride, int problems,
+                           int bc) {
+    EncodeTiledFn enc = encode_tiled();
+    FDADI_REQUIRE(enc != nullptr, "cuTensorMapEncodeTiled is not available from the driver");
+    const bool one = problems == 1;
+    FDADI_REQUIRE(one || stride != 0, "GEMM outputs of several problems need a nonzero stride");
+    cuuint64_t dims[3] = {(cuuint64_t)N, (cuuint64_t)M, (cuuint64_t)problems};
+    cuuint64_t strides[2] = {(cuuint64_t)(ld * esize), (cuuint64_t)((one ? M * ld : stride) * esize)};
+    cuuint32_t box[3] = {(cuuint32_t)bc, 32, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    const int rowb = bc * esize;
+    const CUtensorMapSwizzle sw = rowb == 128 ? CU_TENSOR_MAP_SWIZZLE_128B
+                                : rowb == 64  ? CU_TENSOR_MAP_SWIZZLE_64B
+                                              : CU_TENSOR_MAP_SWIZZLE_32B;
+    const CUresult r = enc(m, type, 3, base, dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    FDADI_REQUIRE(r == CUDA_SUCCESS, "cuTensorMapEncodeTiled (output) failed (%d)", (int)r);
+    return FDADI_OK;
+}
+
 static int launch_ws(const fdadi_gemm_t *a, const GemmArgs &g, cudaStream_t st) {
     static bool attr[64] = {false};
     int dev = 0;
@@ -770,9 +865,23 @@ static int launch_ws(const fdadi_gemm_t *a, const GemmArgs &g, cudaStream_t st) 
     if (rc) return rc;
     rc = make_operand_map(&mB, a->B, a->N, a->K, a->ldb, a->strideB, a->problems, a->N);
     if (rc) return rc;
+    // the epilogue's staged block: 32 rows x bc columns (bc = 16 or 32)
+    const int nparts = a->N >= 64 ? 2 : 1;
+    const int bc = std::min(32, a->N / nparts);
+    CUtensorMap mY = {}, mH = {};
+    if (a->out_f32) {
+        rc = make_output_map(&mY, a->out_f32, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, a->M, a->N,
+                             a->ldo, a->strideO, a->problems, bc);
+        if (rc) return rc;
+    }
+    if (a->out_bf16) {
+        rc = make_output_map(&mH, a->out_bf16, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, a->M, a->N,
+                             a->ldh, a->strideH, a->problems, bc);
+        if (rc) return rc;
+    }
     const int units = w.m_tiles * w.ksplit * w.problems;
     const unsigned grid = (unsigned)std::min(units, sms);
-    umma_gemm_ws_kernel<<<grid, WS_THREADS, WS_SMEM, st>>>(mA, mB, w);
+    umma_gemm_ws_kernel<<<grid, WS_THREADS, WS_SMEM, st>>>(mA, mB, mY, mH, w);
     FDADI_CHECK_LAUNCH();
     return FDADI_OK;
 }

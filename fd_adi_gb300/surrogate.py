@@ -104,16 +104,19 @@ class MLPEnsemble(object):
         return self._bufs[M]
 
     # -- forward --
-    def forward(self, X, M):
+    def forward(self, X, M, keep_preact=True):
         """X: bf16 [M][16] (shared by the members). Returns fp32 [P][M][128]
-        whose first two columns are the scaled residual outputs."""
+        whose first two columns are the scaled residual outputs.
+        keep_preact: also store the hidden layers' fp32 pre-activations (the
+        backward pass needs them; inference does not, which halves the
+        forward's memory traffic)."""
         b = self.bufs(M)
         P = self.P
         A, lda, sA = X, 16, 0
         for li, (K, N) in enumerate(LAYERS):
             last = li == len(LAYERS) - 1
             gemm(A, lda, sA, self.Wb[li], K, N * K, M, N, K, P, bias=self.b[li], sBias=N,
-                 out_f32=b["Y"][li], ldo=N, sO=M * N,
+                 out_f32=b["Y"][li] if (last or keep_preact) else None, ldo=N, sO=M * N,
                  out_bf16=None if last else b["H"][li], ldh=N, sH=M * N,
                  act=0 if last else 1, status=self.status)
             if not last:
@@ -293,7 +296,7 @@ class Surrogate(object):
         if M != M0:
             Q = torch.cat([Q, Q[-1:].expand(M - M0, 9)], 0)
         X, base, inbox = self.feat(Q)
-        Y = self.net.forward(X, M)
+        Y = self.net.forward(X, M, keep_preact=False)
         d = self.dev
         price = torch.empty(M, dtype=torch.float64, device=d)
         delta = torch.empty(M, dtype=torch.float64, device=d)
