@@ -711,16 +711,22 @@ __global__ void featurize_kernel(const double *q, int M, const double *lo, const
         if (!(f[k] >= lo[k] && f[k] <= hi[k])) in = 0;
         X[(int64_t)m * 16 + k] = __float2bfloat16((float)(2.0 * (f[k] - lo[k]) / (hi[k] - lo[k]) - 1.0));
     }
-#pragma unroll
-    for (int k = 8; k < 16; ++k) X[(int64_t)m * 16 + k] = __float2bfloat16(0.0f);
     inbox[m] = in;
     const double kt = kap * T;
     const double vbar = kt > 1e-12 ? th + (v0 - th) * (1.0 - exp(-kt)) / kt : v0;
     const double sv = sqrt(fmax(vbar, 1e-12) * T);
     const double d1 = (log(S / K) + r * T) / sv + 0.5 * sv, d2 = d1 - sv;
     const double n1 = 0.5 * erfc(-d1 * 0.7071067811865476), n2 = 0.5 * erfc(-d2 * 0.7071067811865476);
-    base[2 * (int64_t)m] = (S / K) * n1 - exp(-r * T) * n2;
+    const double b0 = (S / K) * n1 - exp(-r * T) * n2;
+    base[2 * (int64_t)m] = b0;
     base[2 * (int64_t)m + 1] = n1;
+    // derived inputs (functions of the same 8 parameters), roughly in [-1, 1]:
+    // the control variate's price and delta, d1, total std, sqrt(T), mean variance
+    const double g[8] = {4.0 * b0 - 1.0, 2.0 * n1 - 1.0, fmin(1.5, fmax(-1.5, d1 / 3.0)),
+                         3.0 * sv - 1.0, 1.4142135623730951 * sqrt(T) - 1.0, 12.0 * vbar - 1.0,
+                         0.0, 0.0};
+#pragma unroll
+    for (int k = 0; k < 8; ++k) X[(int64_t)m * 16 + 8 + k] = __float2bfloat16((float)g[k]);
 }
 
 // Ensemble read-out: member outputs y[p][m][0..1] (scaled residuals) ->

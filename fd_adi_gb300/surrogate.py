@@ -27,9 +27,9 @@ from . import mesh as _mesh
 BOX_LO = np.array([1 / 1.3, 0.1, 0.0, 0.5, 0.01, 0.1, -0.9, 0.01])
 BOX_HI = np.array([1 / 0.7, 2.0, 0.08, 5.0, 0.16, 1.0, 0.0, 0.16])
 HV_THETA = 0.5 + math.sqrt(3.0) / 6.0
-# (padded input width, padded output width) per layer; 8 inputs, 2 outputs
+# (padded input width, padded output width) per layer; 14 inputs, 2 outputs
 LAYERS = [(16, 256), (256, 256), (256, 256), (256, 256), (256, 128)]
-N_IN, N_OUT = 8, 2
+N_IN, N_OUT = 14, 2   # inputs: 8 parameters + 6 derived (featurize_kernel)
 
 
 def _p(t):
