@@ -41,6 +41,10 @@ class Mixed(ctypes.Structure):
                 ("R", ctypes.c_void_p)]
 
 
+STATUS_PIVOT = 1        # a line-solve pivot was zero or non-finite
+STATUS_NONFINITE = 2    # the option's grid holds a NaN or infinity
+
+
 class HestonPlan(ctypes.Structure):
     """fdadi_heston_plan_t"""
     _fields_ = [("spot_kind", ctypes.c_int32), ("spot_a", ctypes.c_int32),
@@ -121,6 +125,13 @@ SIGNATURES = {
                                          ctypes.POINTER(HestonPlan), ctypes.c_void_p]),
     "fdadi_heston_default_plan": (ctypes.c_int, [ctypes.POINTER(HestonBatch),
                                                  ctypes.POINTER(HestonPlan)]),
+    "fdadi_heston_greeks": (ctypes.c_int, [ctypes.POINTER(HestonBatch), ctypes.c_void_p,
+                                           ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.c_void_p]),
+    "fdadi_heston_status": (ctypes.c_int, [ctypes.POINTER(HestonBatch), ctypes.c_void_p,
+                                           ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.c_void_p]),
     "fdadi_heston_stage": (ctypes.c_int, [ctypes.POINTER(HestonBatch), ctypes.c_void_p,
                                           ctypes.c_int64, ctypes.c_void_p, ctypes.c_int32,
                                           ctypes.c_void_p]),

@@ -236,6 +236,48 @@ class HestonBatch(object):
             torch.cuda.current_stream(self.device).wait_stream(self.stream)
         return V
 
+    def greeks(self, V, flat_idx):
+        """(price, delta, gamma) device tensors: each option's value at its
+        arena index and the centred non-uniform S-derivatives there."""
+        out = [torch.empty(self.n, dtype=torch.float64, device=self.device) for _ in range(3)]
+        cur = torch.cuda.current_stream(self.device)
+        _lib.call("fdadi_heston_greeks", ctypes.byref(self.struct),
+                  ctypes.c_void_p(self.workspace.data_ptr()), self.workspace_bytes,
+                  ctypes.c_void_p(V.data_ptr()), ctypes.c_void_p(flat_idx.data_ptr()),
+                  *[ctypes.c_void_p(t.data_ptr()) for t in out], ctypes.c_void_p(cur.cuda_stream))
+        return tuple(out)
+
+    def status(self, V):
+        """Per-option status words (numpy int32): bit 1 = a line-solve pivot
+        was zero or non-finite when the operators were built, bit 2 = the
+        option's grid in V holds a NaN or infinity."""
+        out = torch.empty(self.n, dtype=torch.int32, device=self.device)
+        with torch.cuda.stream(self.stream):
+            _lib.call("fdadi_heston_status", ctypes.byref(self.struct),
+                      ctypes.c_void_p(self.workspace.data_ptr()), self.workspace_bytes,
+                      ctypes.c_void_p(V.data_ptr()), ctypes.c_void_p(out.data_ptr()),
+                      self._sptr())
+        self.stream.synchronize()
+        return out.cpu().numpy()
+
+    def check(self, V):
+        """Raise ValueError naming the options whose solve failed (the
+        reference raises from DIE() on a failed solve)."""
+        st = self.status(V)
+        bad = np.nonzero(st)[0]
+        if bad.size:
+            what = []
+            for k in bad[:8]:
+                why = []
+                if st[k] & _lib.STATUS_PIVOT:
+                    why.append("zero or non-finite pivot")
+                if st[k] & _lib.STATUS_NONFINITE:
+                    why.append("non-finite values")
+                what.append("option %d: %s" % (k, ", ".join(why)))
+            raise ValueError("%d of %d options failed (%s%s)"
+                             % (bad.size, self.n, "; ".join(what), "; ..." if bad.size > 8 else ""))
+        return st
+
     def solve(self, grids):
         """Host grids in, host grids out."""
         V = self.pack(grids)

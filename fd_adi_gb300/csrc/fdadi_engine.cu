@@ -92,6 +92,7 @@ struct Arena {
     // stage buffers
     double *FV, *W, *T, *Y2;
     const double *theta;       // [n_opt]
+    int *ostat;                // [n_opt] FDADI_STATUS_* bits found while building
 };
 
 // ---- operator rows (reference construction) ------------------------------
@@ -214,12 +215,15 @@ __device__ __forceinline__ void opt_params(const BuildArgs &a, int o, double &r,
 // Thomas factors (a_k, 1/m_k, c'_k) of one line with rows (sub, mid, sup):
 // m_0 = mid_0, m_k = mid_k - sub_k c'_{k-1}, c'_k = sup_k / m_k; stored at
 // L[q], L[stride + q], L[2 stride + q].
+// bad: some pivot m_k was zero or non-finite.
 struct Thomas {
     double cp = 0.0;
+    bool bad = false;
     __device__ __forceinline__ void row(double *L, int64_t stride, int64_t q, double sub, double mid,
                                         double sup, bool first) {
         const double m = first ? mid : mid - sub * cp;
         const double inv = 1.0 / m;
+        if (!isfinite(inv)) bad = true;
         cp = sup * inv;
         L[q] = sub;
         L[stride + q] = inv;
@@ -254,6 +258,7 @@ __device__ void var_factors(const Arena &A, int o, const double *v, int n1, doub
     // S = 0: A1 is (-r/2) I (both variance coefficients vanish there)
     const Row3 z = var_row(v, n1, 0, 0.0, r, half_r, kappa, th, sigma);
     *zinv = 1.0 / ADD(MUL(z.mid, scale), 1.0);
+    if (t.bad || !isfinite(*zinv) || !isfinite(f)) atomicOr(&A.ostat[o], FDADI_STATUS_PIVOT);
 }
 
 __global__ void build_options_kernel(Arena A, BuildArgs a) {
@@ -373,6 +378,7 @@ __global__ void build_spot_lines_kernel(Arena A, BuildArgs a) {
             ti.row(A.LSi, A.P, p, sb, md, sp, i == 0);
         }
     }
+    if (tm.bad || ti.bad) atomicOr(&A.ostat[o], FDADI_STATUS_PIVOT);
 }
 
 // ---- stage kernels --------------------------------------------------------
@@ -936,6 +942,44 @@ __global__ void __launch_bounds__(NW * 32) var_solve_pipe_kernel(Arena A, Span t
     }
 }
 
+// Per-option status: the build's pivot flags, plus FDADI_STATUS_NONFINITE if
+// any value of the option's state grid is NaN or infinite (one block per option).
+__global__ void status_kernel(Arena A, const double *V, int *out) {
+    const int o = blockIdx.x;
+    const int64_t p0 = A.p_off[o], n = (int64_t)A.n0[o] * A.n1[o];
+    int bad = 0;
+    for (int64_t k = threadIdx.x; k < n && !bad; k += blockDim.x)
+        if (!isfinite(V[p0 + k])) bad = 1;
+    bad = __syncthreads_or(bad);
+    if (threadIdx.x == 0) out[o] = A.ostat[o] | (bad ? FDADI_STATUS_NONFINITE : 0);
+}
+
+// Price, delta and gamma of option o at the grid point idx[o] (an index into
+// the packed arena on its spot line): V there and the centred non-uniform first
+// and second derivative stencils in S (centercoeffs, BandedOperator.pyx:970-1017)
+// applied along the spot line; NaN greeks at the first or last spot row.
+__global__ void greeks_kernel(Arena A, const double *spots, const double *V, const int64_t *idx,
+                              double *price, double *delta, double *gamma) {
+    const int o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= A.n_opt) return;
+    const int n0 = A.n0[o], n1 = A.n1[o];
+    const int64_t q = idx[o];
+    const int i = (int)((q - A.p_off[o]) / n1);
+    const double vc = V[q];
+    price[o] = vc;
+    if (i <= 0 || i >= n0 - 1) {
+        delta[o] = gamma[o] = __longlong_as_double(0x7ff8000000000000LL);
+        return;
+    }
+    const double *S = spots + A.s_off[o];
+    const double vm = V[q - n1], vp = V[q + n1];
+    double sb, md, sp;
+    centre(S, i, 1, sb, md, sp);
+    delta[o] = sb * vm + md * vc + sp * vp;
+    centre(S, i, 2, sb, md, sp);
+    gamma[o] = sb * vm + md * vc + sp * vp;
+}
+
 // Eight independent DFMA chains per thread: measures the FP64 pipe, not latency.
 __global__ void fp64_probe_kernel(double *out, int iters) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -968,7 +1012,7 @@ struct Layout {
     int64_t P = 0, SS = 0, SV = 0, n_tiles = 0, n_vtasks = 0;
     bool smoothing = false, hv = false;
     // byte offsets into the workspace (-1: absent)
-    int64_t o_n0, o_n1, o_flags, o_p, o_s, o_v, o_lineS, o_tiles, o_vtasks, o_theta;
+    int64_t o_n0, o_n1, o_flags, o_p, o_s, o_v, o_lineS, o_tiles, o_vtasks, o_theta, o_ostat;
     int64_t o_F0, o_w0, o_w1, o_LS, o_R0top, o_F1v, o_F1x, o_F1z, o_LVv, o_foldV, o_LVz,
         o_dirS;
     int64_t o_w0i, o_RSi, o_LSi, o_LVvi, o_foldVi, o_LVzi;
@@ -1020,6 +1064,7 @@ static int make_layout(const fdadi_heston_batch_t *b, Layout &L) {
     L.o_p = take(8 * N); L.o_s = take(8 * N); L.o_v = take(8 * N);
     L.o_lineS = take(4 * L.SV); L.o_tiles = take(16 * L.n_tiles);
     L.o_vtasks = take(16 * L.n_vtasks); L.o_theta = take(D * N);
+    L.o_ostat = take(4 * N);
     L.o_F0 = take(3 * D * L.P);
     L.o_w0 = take(3 * D * L.SS); L.o_w1 = take(3 * D * L.SV);
     L.o_LS = take(3 * D * L.P); L.o_R0top = take(D * L.SV); L.o_F1v = take(3 * D * L.SV);
@@ -1054,6 +1099,7 @@ static Arena arena_view(const Layout &L, char *ws) {
     A.tiles = (const int4 *)(ws + L.o_tiles);
     A.vtasks = (const int4 *)(ws + L.o_vtasks);
     A.theta = ptr(L.o_theta);
+    A.ostat = (int *)(ws + L.o_ostat);
     A.F0 = ptr(L.o_F0); A.w0 = ptr(L.o_w0); A.w1 = ptr(L.o_w1);
     A.LS = ptr(L.o_LS); A.R0top = ptr(L.o_R0top); A.F1v = ptr(L.o_F1v); A.F1x = ptr(L.o_F1x);
     A.F1z = ptr(L.o_F1z); A.LVv = ptr(L.o_LVv); A.foldV = ptr(L.o_foldV); A.LVz = ptr(L.o_LVz);
@@ -1520,6 +1566,7 @@ int fdadi_heston_prepare(const fdadi_heston_batch_t *b, void *workspace, int64_t
     FDADI_CUDA(cudaMemcpyAsync(ws + L.o_tiles, tiles.data(), 16 * tiles.size(), cudaMemcpyHostToDevice, st));
     FDADI_CUDA(cudaMemcpyAsync(ws + L.o_vtasks, vtasks.data(), 16 * vtasks.size(), cudaMemcpyHostToDevice, st));
     FDADI_CUDA(cudaMemcpyAsync(ws + L.o_theta, theta.data(), 8 * L.n_opt, cudaMemcpyHostToDevice, st));
+    FDADI_CUDA(cudaMemsetAsync(ws + L.o_ostat, 0, 4 * L.n_opt, st));
     Arena A = arena_view(L, ws);
     BuildArgs a{b->spots, b->vars, b->params, b->dt, b->barrier, b->theta, b->implicit_dt_factor,
                 L.smoothing ? 1 : 0, (b->flags & FDADI_HESTON_DROP_ZERO_MIXED) ? 1 : 0,
@@ -1600,6 +1647,37 @@ int fdadi_heston_stage(const fdadi_heston_batch_t *b, void *workspace, int64_t w
     rc = grids(b, L, g);
     if (rc) return rc;
     launch_stage(stage, g, A, V, as_stream(stream));
+    FDADI_CHECK_LAUNCH();
+    return FDADI_OK;
+}
+
+int fdadi_heston_status(const fdadi_heston_batch_t *b, void *workspace, int64_t ws_bytes,
+                        const double *V, int32_t *status, void *stream) {
+    Layout L;
+    int rc = make_layout(b, L);
+    if (rc) return rc;
+    rc = check_ws(L, workspace, ws_bytes);
+    if (rc) return rc;
+    FDADI_REQUIRE(V != nullptr && status != nullptr, "null state or status array");
+    Arena A = arena_view(L, (char *)workspace);
+    status_kernel<<<(unsigned)L.n_opt, 256, 0, as_stream(stream)>>>(A, V, status);
+    FDADI_CHECK_LAUNCH();
+    return FDADI_OK;
+}
+
+int fdadi_heston_greeks(const fdadi_heston_batch_t *b, void *workspace, int64_t ws_bytes,
+                        const double *V, const int64_t *flat_index, double *price, double *delta,
+                        double *gamma, void *stream) {
+    Layout L;
+    int rc = make_layout(b, L);
+    if (rc) return rc;
+    rc = check_ws(L, workspace, ws_bytes);
+    if (rc) return rc;
+    FDADI_REQUIRE(V && flat_index && price && delta && gamma && b->spots,
+                  "null greeks argument");
+    Arena A = arena_view(L, (char *)workspace);
+    greeks_kernel<<<(unsigned)((L.n_opt + 127) / 128), 128, 0, as_stream(stream)>>>(
+        A, b->spots, V, flat_index, price, delta, gamma);
     FDADI_CHECK_LAUNCH();
     return FDADI_OK;
 }

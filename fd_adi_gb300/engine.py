@@ -325,6 +325,78 @@ class FiniteDifferenceEngineADI(FiniteDifferenceEngine):
                 Li.solve_(V, overwrite=True)
         return V
 
+    def solve_craigsneyd_(self, n, dt, V, theta=0.5, modified=False):
+        """Craig-Sneyd (FiniteDifference.pyx:843-898) or, with modified, the
+        modified Craig-Sneyd scheme (:779-841), on device arrays. Per step:
+        Y0 = V + sum F_k V; Y2 from the Douglas sweep; then Z = Y0 +
+        (dt/2) M (Y2 - V) (modified: theta dt M (Y2 - V) + (1/2 - theta)
+        sum F_k.apply(Y2 - V), residuals included as the reference applies
+        them), and the same sweep from Z. The reference has these on the CPU
+        engine only; they run here on the per-operator kernels."""
+        dt, theta = float(dt), float(theta)
+        if not self.operators:
+            self.scale_and_combine_operators()
+        Firsts = [o.mul_scalar_from_host(dt) for d, o in self.operators.items()]
+        dims = self._dims()
+        Les = [o.mul_scalar_from_host(theta).mul_scalar_from_host(dt, inplace=True)
+               for d, o in dims]
+        Lis = [o.mul_scalar_from_host(theta * -dt).add(1, inplace=True) for d, o in dims]
+        for L in Les + Lis:
+            L.enable_residual(False)
+        for L in Les + Lis + Firsts:
+            if L.is_foldable():
+                L.diagonalize()
+        cross = self.operators.get((0, 1))
+        c = theta * dt if modified else 0.5 * dt
+        X = torch.empty_like(V)
+        Y = torch.empty_like(V)
+        Y0 = torch.empty_like(V)
+        D = torch.empty_like(V)
+        for _ in range(int(n)):
+            Y.copy_(V)
+            for L in Firsts:
+                _apply_into(L, X, V)
+                _axpby(Y, X, 1.0, 1.0)
+            Y0.copy_(Y)
+            for Le, Li in zip(Les, Lis):
+                _apply_into(Le, X, V)
+                _axpby(Y, X, 1.0, -1.0)
+                Li.solve_(Y, overwrite=True)
+            D.copy_(Y)
+            _axpby(D, V, 1.0, -1.0)          # D = Y2 - V
+            Y.copy_(Y0)
+            if cross is not None:
+                _apply_into(cross, X, D)
+                _axpby(Y, X, 1.0, c)
+            if modified:
+                for L in Firsts:
+                    _apply_into(L, X, D)
+                    _axpby(Y, X, 1.0, 0.5 - theta)
+            for Le, Li in zip(Les, Lis):
+                _apply_into(Le, X, V)
+                _axpby(Y, X, 1.0, -1.0)
+                Li.solve_(Y, overwrite=True)
+            V.copy_(Y)
+        return V
+
+    def solve_craigsneyd2_(self, n, dt, V, theta=0.5):
+        """Modified Craig-Sneyd (FiniteDifference.pyx:779-841)."""
+        return self.solve_craigsneyd_(n, dt, V, theta, modified=True)
+
+    def solve_craigsneyd(self, n, dt, initial=None, theta=0.5, callback=None, numpy=False):
+        if callback or numpy:
+            raise NotImplementedError("Callbacks and Numpy not available for GPU solver.")
+        V = self._initial(initial)
+        self.solve_craigsneyd_(int(n), dt, V, theta)
+        return V.cpu().numpy()
+
+    def solve_craigsneyd2(self, n, dt, initial=None, theta=0.5, callback=None, numpy=False):
+        if callback or numpy:
+            raise NotImplementedError("Callbacks and Numpy not available for GPU solver.")
+        V = self._initial(initial)
+        self.solve_craigsneyd_(int(n), dt, V, theta, modified=True)
+        return V.cpu().numpy()
+
     def solve_smooth_(self, n, dt, V, smoothing_steps=2):
         """Rannacher start: 2*s implicit half-steps, then HV at theta = 0.6
         (FiniteDifferenceEngine.pyx:1010-1016)."""

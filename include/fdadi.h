@@ -252,6 +252,26 @@ int fdadi_heston_tune(const fdadi_heston_batch_t *batch, void *workspace,
                       int64_t workspace_bytes, int32_t reps, fdadi_heston_plan_t *plan,
                       void *stream);
 
+/* Per-option status words (the reference raises from DIE() on a failed solve,
+ * common.h:17-27; a batch reports per option instead). */
+#define FDADI_STATUS_PIVOT 1      /* a line-solve pivot of the option was zero or non-finite */
+#define FDADI_STATUS_NONFINITE 2  /* the option's state grid holds a NaN or infinity */
+/* status[k] (DEVICE, int32 [n_options]) = the FDADI_STATUS_* bits of option k:
+ * pivot flags recorded by fdadi_heston_prepare, plus a scan of the state V
+ * (DEVICE, the packed arena) for non-finite values. */
+int fdadi_heston_status(const fdadi_heston_batch_t *batch, void *workspace,
+                        int64_t workspace_bytes, const double *V, int32_t *status, void *stream);
+
+/* Price, delta and gamma of every option at its grid point flat_index[k]
+ * (DEVICE int64 [n_options], an index into the packed arena inside option k's
+ * grid): V there and the centred non-uniform first and second derivatives in
+ * S along the spot line (the reference's centercoeffs stencils,
+ * BandedOperator.pyx:970-1017). Greeks are NaN on the first and last spot rows.
+ * Outputs are DEVICE double [n_options]. */
+int fdadi_heston_greeks(const fdadi_heston_batch_t *batch, void *workspace,
+                        int64_t workspace_bytes, const double *V, const int64_t *flat_index,
+                        double *price, double *delta, double *gamma, void *stream);
+
 /* The plan fdadi_heston_run uses for this batch when batch->plan is NULL. */
 int fdadi_heston_default_plan(const fdadi_heston_batch_t *batch, fdadi_heston_plan_t *plan);
 

@@ -595,13 +595,82 @@ static void run_implicit(const engine_t *E, int n, double dt, double *V) {
     for (int d = 0; d < nd; ++d) op_free(Li[d]);
 }
 
-enum { SCHEME_IMPLICIT = 0, SCHEME_DOUGLAS = 1, SCHEME_HV = 2 };
+/* Craig-Sneyd, FiniteDifferenceEngine.pyx:843-898 (modified = 0), and the
+ * modified Craig-Sneyd scheme, :779-841 (modified = 1). Per step:
+ *   Y0 = V + sum_k F_k V (F_k = dt A_k with their residuals, and dt M),
+ *   Y2 = the Douglas sweep from Y0 (Y <- Li_d^-1 (Y - Le_d V), d = 0, 1),
+ *   CS:  Z = Y0 + (dt/2) M (Y2 - V);
+ *   MCS: Z = Y0 + theta dt M (Y2 - V) + (1/2 - theta) sum_k F_k.apply(Y2 - V)
+ *        (the reference applies F_k with its residual here, so it is added),
+ *   then the same sweep from Z, and V <- the result. The reference solves the
+ *   unfolded banded systems with LAPACK; the folded Thomas solve here is the
+ *   same linear system. */
+static void run_cs(const engine_t *E, int n, double dt, double theta, double *V, int modified) {
+    int nd = E->ndim;
+    size_t N = (size_t)E->n0 * E->n1;
+    op_t *F[3], *Le[2], *Li[2];
+    int nf = 0;
+    for (int d = 0; d < nd; ++d) F[nf++] = op_mul(E->A[d], dt);
+    if (E->M) F[nf++] = op_mul(E->M, dt);
+    for (int d = 0; d < nd; ++d) {
+        op_t *t = op_mul(E->A[d], theta);
+        Le[d] = op_mul(t, dt);
+        op_free(t);
+        Li[d] = op_mul(E->A[d], theta * -dt);
+        op_add_scalar_f32(Li[d], 1.0);
+        Le[d]->has_R = 0; Li[d]->has_R = 0;
+    }
+    for (int d = 0; d < nd; ++d) {
+        if (op_foldable(Le[d])) op_diagonalize(Le[d]);
+        if (op_foldable(Li[d])) op_diagonalize(Li[d]);
+    }
+    for (int k = 0; k < nf; ++k) if (op_foldable(F[k]) && !F[k]->mixed) op_diagonalize(F[k]);
+    double *Y = (double *)malloc(N * sizeof(double)), *Y0 = (double *)malloc(N * sizeof(double)),
+           *D = (double *)malloc(N * sizeof(double)), *T = (double *)malloc(N * sizeof(double));
+    for (int s = 0; s < n; ++s) {
+        memcpy(Y, V, N * sizeof(double));
+        for (int k = 0; k < nf; ++k) { op_apply(F[k], V, E->n0, E->n1, T); vadd(Y, T, N); }
+        memcpy(Y0, Y, N * sizeof(double));
+        for (int d = 0; d < nd; ++d) {
+            op_apply(Le[d], V, E->n0, E->n1, T);
+            vsub(Y, T, N);
+            op_solve(Li[d], Y, E->n0, E->n1);
+        }
+        for (size_t i = 0; i < N; ++i) D[i] = Y[i] - V[i];
+        if (E->M) {
+            op_apply(E->M, D, E->n0, E->n1, T);
+            const double c = modified ? theta * dt : 0.5 * dt;
+            for (size_t i = 0; i < N; ++i) Y[i] = Y0[i] + c * T[i];
+        } else {
+            memcpy(Y, Y0, N * sizeof(double));
+        }
+        if (modified) {
+            for (int k = 0; k < nf; ++k) {
+                op_apply(F[k], D, E->n0, E->n1, T);
+                for (size_t i = 0; i < N; ++i) Y[i] += (0.5 - theta) * T[i];
+            }
+        }
+        for (int d = 0; d < nd; ++d) {
+            op_apply(Le[d], V, E->n0, E->n1, T);
+            vsub(Y, T, N);
+            op_solve(Li[d], Y, E->n0, E->n1);
+        }
+        memcpy(V, Y, N * sizeof(double));
+    }
+    free(Y); free(Y0); free(D); free(T);
+    for (int k = 0; k < nf; ++k) op_free(F[k]);
+    for (int d = 0; d < nd; ++d) { op_free(Le[d]); op_free(Li[d]); }
+}
+
+enum { SCHEME_IMPLICIT = 0, SCHEME_DOUGLAS = 1, SCHEME_HV = 2, SCHEME_CS = 3, SCHEME_MCS = 4 };
 
 static void run_schedule(const engine_t *E, int nseg, const int *scheme, const int *nsteps,
                          const double *dt, const double *theta, double *V) {
     for (int s = 0; s < nseg; ++s) {
         if (scheme[s] == SCHEME_IMPLICIT) run_implicit(E, nsteps[s], dt[s], V);
         else if (scheme[s] == SCHEME_DOUGLAS) run_douglas(E, nsteps[s], dt[s], theta[s], V);
+        else if (scheme[s] == SCHEME_CS) run_cs(E, nsteps[s], dt[s], theta[s], V, 0);
+        else if (scheme[s] == SCHEME_MCS) run_cs(E, nsteps[s], dt[s], theta[s], V, 1);
         else run_hv(E, nsteps[s], dt[s], theta[s], V);
     }
 }
@@ -609,7 +678,8 @@ static void run_schedule(const engine_t *E, int nseg, const int *scheme, const i
 /* ---- exported entry points (ctypes) ------------------------------------ */
 
 /* One Heston solve on a given mesh. V: [nS*nv] initial grid in, final out.
- * Segments run in order: scheme 0 implicit, 1 Douglas, 2 Hundsdorfer-Verwer. */
+ * Segments run in order: scheme 0 implicit, 1 Douglas, 2 Hundsdorfer-Verwer,
+ * 3 Craig-Sneyd, 4 modified Craig-Sneyd. */
 int oracle_heston_solve(const double *S, int nS, const double *v, int nv,
                         double r, double kappa, double theta, double sigma, double rho,
                         int drop_zero_mixed,

@@ -17,7 +17,8 @@ SRC = os.path.join(HERE, "fdadi_oracle.c")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "liboracle.so")
 
-SCHEMES = {"implicit": 0, "douglas": 1, "hv": 2, "hundsdorferverwer": 2}
+SCHEMES = {"implicit": 0, "douglas": 1, "hv": 2, "hundsdorferverwer": 2,
+           "cs": 3, "craigsneyd": 3, "mcs": 4, "craigsneyd2": 4}
 
 _lib = None
 

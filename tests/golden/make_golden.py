@@ -106,6 +106,10 @@ SCHEDULES = {
                                       [("implicit", n, dt, 1.0)]),
     "smooth": lambda F, n, dt, V0: (H.quiet(F.solve_smooth, n, dt, initial=V0, smoothing_steps=1),
                                     [("implicit", 2, dt * 0.5, 1.0), ("hv", n - 1, dt, 0.6)]),
+    "cs": lambda F, n, dt, V0: (H.quiet(F.solve_craigsneyd, n, dt, initial=V0, theta=0.5),
+                                [("cs", n, dt, 0.5)]),
+    "mcs": lambda F, n, dt, V0: (H.quiet(F.solve_craigsneyd2, n, dt, initial=V0, theta=1.0 / 3),
+                                 [("mcs", n, dt, 1.0 / 3)]),
 }
 
 

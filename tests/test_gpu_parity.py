@@ -172,7 +172,7 @@ def test_barrier_option_vs_host_engine(cuda):
     assert np.abs(a[-1]).max() < 1e-12 * np.abs(a).max()
 
 
-@pytest.mark.parametrize("scheme", ["douglas", "hv", "implicit", "smooth"])
+@pytest.mark.parametrize("scheme", ["douglas", "hv", "implicit", "smooth", "cs", "mcs"])
 def test_plain_engine_vs_oracle(cuda, golden, scheme):
     """The per-operator path (the reference's call sequence) vs the oracle."""
     from fd_adi_gb300 import HestonOption, HestonFiniteDifferenceEngine, Grid
@@ -186,7 +186,9 @@ def test_plain_engine_vs_oracle(cuda, golden, scheme):
     fn = {"douglas": lambda: F.solve_douglas(20, 0.01, theta=0.5),
           "hv": lambda: F.solve_hundsdorferverwer(20, 0.01, theta=HV_THETA),
           "implicit": lambda: F.solve_implicit(20, 0.01),
-          "smooth": lambda: F.solve_smooth(20, 0.01, smoothing_steps=1)}[scheme]
+          "smooth": lambda: F.solve_smooth(20, 0.01, smoothing_steps=1),
+          "cs": lambda: F.solve_craigsneyd(20, 0.01, theta=0.5),
+          "mcs": lambda: F.solve_craigsneyd2(20, 0.01, theta=1.0 / 3)}[scheme]
     out = fn()
     ref = g["c1_" + scheme]
     assert _rel(out, ref) < 1e-11

@@ -200,3 +200,56 @@ def test_tuned_graph_run(uneven):
     out = gb.solve(V0)
     for k in range(len(opts)):
         np.testing.assert_array_equal(out[k], direct[k])
+
+
+def test_status_flags_failed_options(uneven):
+    """Per-option status: a NaN volatility of variance breaks that option's
+    variance-line pivots, a NaN step poisons its grid; the other options
+    report 0 and keep their oracle results."""
+    from fd_adi_gb300 import _lib
+    from fd_adi_gb300.batch import HestonBatch
+    opts, meshes, V0, ref, kw = uneven
+    params = [o.params() for o in opts[:4]]
+    params[1] = params[1][:3] + (float("nan"),) + params[1][4:]
+    dts = list(kw["dt"][:4])
+    dts[2] = float("nan")
+    b = HestonBatch(params, meshes[:4], **dict(kw, dt=dts))
+    V = b.pack(V0[:4])
+    b.run(V)
+    st = b.status(V)
+    assert st[0] == 0 and st[3] == 0
+    assert st[1] & _lib.STATUS_PIVOT
+    assert st[2] & _lib.STATUS_NONFINITE
+    with pytest.raises(ValueError, match="option 1"):
+        b.check(V)
+    out = b.unpack(V)
+    for k in (0, 3):
+        assert _rel(out[k], ref[k]) < 1e-9
+
+
+def test_greeks_match_host_stencils(uneven):
+    """Device delta/gamma at each option's price point against the centred
+    non-uniform stencils applied to the returned grid on the host."""
+    from fd_adi_gb300 import mesh as M
+    from fd_adi_gb300.batch import HestonBatch
+    opts, meshes, V0, ref, kw = uneven
+    b = HestonBatch(opts, meshes, **kw)
+    V = b.pack(V0)
+    b.run(V)
+    idx = b.flat_index()
+    p, d, g = (t.cpu().numpy() for t in b.greeks(V, idx))
+    out = b.unpack(V)
+    for k in range(len(opts)):
+        S, v = meshes[k]
+        i, j = M.price_index(S, v, 100., opts[k].variance.value)
+        di, dn = S[i] - S[i - 1], S[i + 1] - S[i]
+        s = di + dn
+        w1 = (-dn / (di * s), (-di + dn) / (di * dn), di / (dn * s))
+        w2 = (2.0 / (di * s), -2.0 / (di * dn), 2.0 / (dn * s))
+        col = out[k][i - 1:i + 2, j]
+        assert p[k] == out[k][i, j]
+        assert abs(d[k] - np.dot(w1, col)) <= 1e-12 * max(1.0, abs(d[k]))
+        assert abs(g[k] - np.dot(w2, col)) <= 1e-10 * max(1.0, abs(g[k]))
+        # against the oracle's grid: the north-star price bar, delta alike
+        cr = ref[k][i - 1:i + 2, j]
+        assert abs(d[k] - np.dot(w1, cr)) <= 1e-9 * max(1.0, abs(d[k]))

@@ -39,10 +39,12 @@ SCHED = {
     "hv": lambda n, dt: [("hv", n, dt, HV_THETA)],
     "implicit": lambda n, dt: [("implicit", n, dt, 1.0)],
     "smooth": lambda n, dt: [("implicit", 2, dt * 0.5, 1.0), ("hv", n - 1, dt, 0.6)],
+    "cs": lambda n, dt: [("cs", n, dt, 0.5)],
+    "mcs": lambda n, dt: [("mcs", n, dt, 1.0 / 3)],
 }
 
 
-@pytest.mark.parametrize("case", range(12))
+@pytest.mark.parametrize("case", range(18))
 def test_solves_match_reference(golden, case):
     g = golden("solves")
     key = str(g["cases"][case])
