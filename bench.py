@@ -699,6 +699,14 @@ def main():
                              "peak_source": "measured live (fdadi_fp64_probe, DFMA only)",
                              "flops_per_point": STAGE_FLOPS[dom]},
                "stage_ms": {k: round(v[0], 4) for k, v in st.items()},
+               # per stage: algorithmic GB/s (state bytes per point x points /
+               # launch time) against the HBM copy peak, and the FP64 pipe's share
+               "stage_gbs": {k: round(STAGE_BYTES[k] * P / (v[0] * 1e-3) / 1e9, 1)
+                             for k, v in st.items()},
+               "stage_hbm_frac": {k: round(STAGE_BYTES[k] * P / (v[0] * 1e-3) / 1e9 / hbm_peak, 4)
+                                  for k, v in st.items()},
+               "stage_fp64_frac": {k: round(STAGE_FLOPS[k] * P / (v[0] * 1e-3) / 1e12 / fp64, 4)
+                                   for k, v in st.items()},
                "plan": dict(batch.plan, tuned=not (args.no_tune or args.plan),
                             setup_s=round(t_tune, 2)),
                "clocks": clk}

@@ -12,7 +12,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libfdadi.so")
 FDADI_CANNOT_FOLD, FDADI_CAN_FOLD, FDADI_FOLDED = 0, 1, 2
 FOLD_CODES = {"CANNOT_FOLD": 0, "CAN_FOLD": 1, "FOLDED": 2}
 FOLD_NAMES = {v: k for k, v in FOLD_CODES.items()}
-SCHEME_IMPLICIT, SCHEME_DOUGLAS, SCHEME_HV = 0, 1, 2
+SCHEME_IMPLICIT, SCHEME_DOUGLAS, SCHEME_HV, SCHEME_CS, SCHEME_MCS = 0, 1, 2, 3, 4
 HESTON_DROP_ZERO_MIXED, HESTON_GRAPH = 1, 2
 NOALLOC_MAX_ROWS = 1 << 20
 

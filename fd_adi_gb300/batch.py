@@ -19,7 +19,8 @@ from . import _lib
 from . import mesh as _mesh
 
 SCHEMES = {"douglas": _lib.SCHEME_DOUGLAS, "hv": _lib.SCHEME_HV,
-           "hundsdorferverwer": _lib.SCHEME_HV}
+           "hundsdorferverwer": _lib.SCHEME_HV, "cs": _lib.SCHEME_CS,
+           "craigsneyd": _lib.SCHEME_CS, "mcs": _lib.SCHEME_MCS, "craigsneyd2": _lib.SCHEME_MCS}
 HV_THETA = 0.5 + np.sqrt(3.0) / 6.0
 
 
@@ -28,12 +29,14 @@ HV_THETA = 0.5 + np.sqrt(3.0) / 6.0
 # partitioned lines, lines per block, segments per line) and variance solve
 # (kind 0: one tile per warp, factors loaded in the recurrence; kind 1: two
 # tiles, pipelined copies, factors by shuffle; kind 2: one tile, factors by
-# shuffle; warps per block).
+# shuffle; warps per block; kind 3: partitioned lines, one 32-row task per
+# block split into column segments, warps per block).
 SPOT_PLANS = [(0, 1, 128), (0, 1, 64), (0, 1, 256), (0, 4, 32), (0, 8, 32), (0, 8, 64),
               (1, 32, 4), (1, 32, 8), (1, 32, 16), (1, 32, 32), (1, 16, 16), (1, 16, 32),
               (1, 16, 64), (1, 8, 32), (1, 8, 64), (1, 8, 128), (0, 2, 64), (0, 2, 128),
               (0, 4, 64), (0, 4, 128)]
-VAR_PLANS = [(0, 4), (0, 2), (1, 1), (1, 2), (1, 4), (2, 1), (2, 2), (2, 4)]
+VAR_PLANS = [(0, 4), (0, 2), (1, 1), (1, 2), (1, 4), (2, 1), (2, 2), (2, 4), (3, 4), (3, 8),
+             (3, 16)]
 
 
 def make_plan(spot, var, groups=1, expl_per_sm=0):
@@ -89,7 +92,7 @@ class HestonBatch(object):
     meshes:  list of (spots, vars) numpy arrays, one per option.
     dt:      per-option main step (scalar or sequence).
     Schedule: ``implicit_steps`` fully implicit steps of dt*implicit_dt_factor,
-    then ``n_steps`` of ``scheme`` ("douglas" or "hv") at ``theta``.
+    then ``n_steps`` of ``scheme`` ("douglas", "hv", "cs" or "mcs") at ``theta``.
     plan:    launch plan of the line solves: None (size heuristic), "auto"
              (measured by the autotuner on this batch, cached by batch shape)
              or a dict of fdadi_heston_plan_t fields."""

@@ -383,14 +383,16 @@ __global__ void build_spot_lines_kernel(Arena A, BuildArgs a) {
 
 // ---- stage kernels --------------------------------------------------------
 
-enum : int { ST_DOUGLAS = 0, ST_HV0 = 1, ST_HV3 = 2, ST_IMPLICIT = 3 };
+enum : int { ST_DOUGLAS = 0, ST_HV0 = 1, ST_HV3 = 2, ST_IMPLICIT = 3, ST_CS3 = 4, ST_MCS3 = 5 };
 
 // One 16x32 tile of one option. X (the operand of the applies: V, or Y2 in
 // the HV corrector) is staged with a halo of one row above and below, two
 // columns on the left (the A[n1-1, n1-3] corner) and one on the right.
 template <int MODE>
 __device__ __forceinline__ void explicit_tile(const Arena &A, const double *__restrict__ V,
-                                              int64_t tile, double (*sX)[XCP], double (*sT)[TJ]) {
+                                              int64_t tile, double (*sX)[XCP], double (*sT)[TJ],
+                                              double (*sD)[XCP]) {
+    constexpr bool CS = MODE == ST_CS3 || MODE == ST_MCS3;
     const int4 t = A.tiles[tile];
     const int o = t.x, i0 = t.y, j0 = t.z;
     const int n0 = A.n0[o], n1 = A.n1[o];
@@ -401,20 +403,26 @@ __device__ __forceinline__ void explicit_tile(const Arena &A, const double *__re
     for (int e = tid; e < XR * XC; e += EXPL_THREADS) {
         const int rr = e / XC, cc = e - rr * XC;
         const int ii = i0 - 1 + rr, jj = j0 - 2 + cc;
-        sX[rr][cc] = (ii >= 0 && ii < n0 && jj >= 0 && jj < n1) ? X[(int64_t)ii * n1 + jj] : 0.0;
+        const bool in = ii >= 0 && ii < n0 && jj >= 0 && jj < n1;
+        const double x = in ? X[(int64_t)ii * n1 + jj] : 0.0;
+        sX[rr][cc] = x;
+        // Craig-Sneyd correctors: D = Y2 - V beside V
+        if constexpr (CS) sD[rr][cc] = in ? A.Y2[p0 + (int64_t)ii * n1 + jj] - x : 0.0;
     }
     __syncthreads();
     const bool mixed = fl & OPT_MIXED;
     const int64_t vo = A.v_off[o], so = A.s_off[o];
     if (mixed) {
-        // mixed stencil row sums t(r, j) = sum_b w1[b](j) X(r, j + b)
+        // mixed stencil row sums t(r, j) = sum_b w1[b](j) X(r, j + b) (of D in
+        // the Craig-Sneyd correctors)
+        double(*sM)[XCP] = CS ? sD : sX;
         for (int e = tid; e < XR * TJ; e += EXPL_THREADS) {
             const int rr = e / TJ, cc = e - rr * TJ;
             const int jj = j0 + cc;
             double s = 0.0;
             if (jj > 0 && jj < n1 - 1)
-                s = A.w1[vo + jj] * sX[rr][cc + 1] + A.w1[A.SV + vo + jj] * sX[rr][cc + 2] +
-                    A.w1[2 * A.SV + vo + jj] * sX[rr][cc + 3];
+                s = A.w1[vo + jj] * sM[rr][cc + 1] + A.w1[A.SV + vo + jj] * sM[rr][cc + 2] +
+                    A.w1[2 * A.SV + vo + jj] * sM[rr][cc + 3];
             sT[rr][cc] = s;
         }
         __syncthreads();
@@ -428,6 +436,51 @@ __device__ __forceinline__ void explicit_tile(const Arena &A, const double *__re
 
     const bool mix_pt = mixed && i > 0 && i < n0 - 1 && j > 0 && j < n1 - 1;
     const double xc = sX[ty + 1][tx + 2];
+    if constexpr (CS) {
+        // Craig-Sneyd corrector (FiniteDifferenceEngine.pyx:843-898): right-hand
+        // side of the second sweep, Y0 + (dt/2) M D - theta dt A0 V with
+        // Y0 = V + R + F(V) and D = Y2 - V. Modified (:779-841): theta dt M D +
+        // (1/2 - theta) sum_k F_k.apply(D) in place of (dt/2) M D, which is
+        // (dt/2) M D + (1/2 - theta)(dt A0 D + dt A1 D + dt R): the reference
+        // applies F_k with its residual. T = dt A1 V for the variance sweep.
+        const double th = A.theta[o];
+        const double gl = A.dirS[js], gh = A.dirS[A.SV + js];
+        const bool dlo = i == 0 && slow, dhi = i == n0 - 1 && shigh;
+        auto spot_apply = [&](double (*sY)[XCP], const double *F) {
+            if (dlo) return gl;
+            if (dhi) return gh;
+            const double ym = (i == 1 && slow) ? gl : sY[ty][tx + 2];
+            const double yp = (i == n0 - 2 && shigh) ? gh : sY[ty + 2][tx + 2];
+            return F[p] * ym + F[P + p] * sY[ty + 1][tx + 2] + F[2 * P + p] * yp;
+        };
+        auto var_apply = [&](double (*sY)[XCP]) {
+            const double yc = sY[ty + 1][tx + 2];
+            if (i == 0 && (fl & OPT_ROW0_ZERO)) return A.F1z[o] * yc;
+            double r = A.F1v[js] * sY[ty + 1][tx + 1] + A.F1v[A.SV + js] * yc +
+                       A.F1v[2 * A.SV + js] * sY[ty + 1][tx + 3];
+            if (j == n1 - 1) r += A.F1x[o] * sY[ty + 1][tx];
+            return r;
+        };
+        const double a0v = spot_apply(sX, A.F0), a1v = var_apply(sX);
+        double acc = xc + A.FV[p];
+        if (i == n0 - 1) acc = fma(MODE == ST_CS3 ? 1.0 : 1.5 - th, A.R0top[js], acc);
+        acc = fma(-th, a0v, acc);
+        if (mix_pt) {
+            acc = fma(A.w0h[so + i], sT[ty][tx], acc);
+            acc = fma(A.w0h[A.SS + so + i], sT[ty + 1][tx], acc);
+            acc = fma(A.w0h[2 * A.SS + so + i], sT[ty + 2][tx], acc);
+        }
+        if constexpr (MODE == ST_MCS3) {
+            // (1/2 - theta) dt A0 D through the (1/2 - theta) F0 copy; Dirichlet
+            // rows give the boundary value, as apply does
+            const double a0d = (dlo || dhi) ? (0.5 - th) * (dlo ? gl : gh) : spot_apply(sD, A.F0h);
+            acc += a0d;
+            acc = fma(0.5 - th, var_apply(sD), acc);
+        }
+        A.W[p] = acc;
+        A.T[p] = a1v;
+        return;
+    }
     if constexpr (MODE == ST_HV3) {
         // Y0 - F(V - Y2)/2 - theta F0 Y2 = V + R + F(V)/2 + (1/2 - theta) F0 Y2
         //   + F1 Y2 / 2 + M Y2 / 2, accumulated in one FMA chain with the
@@ -516,8 +569,9 @@ __global__ void __launch_bounds__(EXPL_THREADS, 4) explicit_kernel(Arena A, cons
                                                                   int64_t tile0, int64_t tile1) {
     __shared__ double sX[XR][XCP];
     __shared__ double sT[XR][TJ];
+    __shared__ double sD[(MODE == ST_CS3 || MODE == ST_MCS3) ? XR : 1][XCP];
     for (int64_t t = tile0 + blockIdx.x; t < tile1; t += gridDim.x) {
-        explicit_tile<MODE>(A, V, t, sX, sT);
+        explicit_tile<MODE>(A, V, t, sX, sT, sD);
         __syncthreads();  // the next tile reuses the shared tiles
     }
 }
@@ -942,6 +996,171 @@ __global__ void __launch_bounds__(NW * 32) var_solve_pipe_kernel(Arena A, Span t
     }
 }
 
+// Partitioned variance solve, for few long variance lines (one large grid):
+// one block per task of up to 32 grid rows, its NSEG warps each taking a
+// contiguous range of 32-column chunks. As in spot_seg_kernel, each segment
+// runs both Thomas recurrences from a zero carry while tracking the product
+// of the multipliers, warp 0 combines the segment carries per row, and a
+// second pass adds product x carry; every pass streams its chunks through the
+// warp's padded shared tile (coalesced rows, lane = grid row in the
+// recurrence) with the factors broadcast by shuffle. Dynamic shared memory:
+// NSEG * 32 * VS_PITCH doubles.
+template <bool IMPLICIT, int NSEG>
+__global__ void __launch_bounds__(NSEG * 32) var_seg_kernel(Arena A, Span tasks,
+                                                            const double *src, double *dst) {
+    extern __shared__ double vsm[];
+    __shared__ double cval[NSEG][32], cwt[NSEG][32];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t task = tasks.lo + blockIdx.x;   // grid = tasks.hi - tasks.lo
+    double(*tl)[VS_PITCH] = reinterpret_cast<double(*)[VS_PITCH]>(vsm + (size_t)warp * 32 * VS_PITCH);
+    const int4 tk = A.vtasks[task];
+    const int o = tk.x, i0 = tk.y, rows = tk.z;
+    const int n1 = A.n1[o];
+    const int64_t base = A.p_off[o] + (int64_t)i0 * n1;
+    const int64_t vo = A.v_off[o], SV = A.SV;
+    const double *L = IMPLICIT ? A.LVvi : A.LVv;
+    const double f = IMPLICIT ? A.foldVi[o] : A.foldV[o];
+    const double z = IMPLICIT ? A.LVzi[o] : A.LVz[o];
+    const bool special = (i0 + lane == 0) && (A.oflags[o] & OPT_ROW0_ZERO);
+    const unsigned FULL = 0xffffffffu;
+    const int nch = (n1 + 31) >> 5;
+    const int cps = (nch + NSEG - 1) / NSEG;
+    const int ch_lo = min(nch, warp * cps), ch_hi = min(nch, ch_lo + cps);
+    // raw right-hand side at column n1 - 2 (the bottom fold adds it to the last
+    // column), read before any write since src and dst may alias
+    double rfold = 0.0;
+    if (lane < rows) rfold = src[base + (int64_t)lane * n1 + n1 - 2];
+    __syncthreads();
+    auto load = [&](const double *from, int ch) {
+        const int c0 = ch << 5, w = min(32, n1 - c0);
+        if (lane < w)
+            for (int rr = 0; rr < rows; ++rr) tl[rr][lane] = from[base + (int64_t)rr * n1 + c0 + lane];
+        __syncwarp();
+    };
+    auto store = [&](int ch) {
+        __syncwarp();
+        const int c0 = ch << 5, w = min(32, n1 - c0);
+        if (lane < w)
+            for (int rr = 0; rr < rows; ++rr) dst[base + (int64_t)rr * n1 + c0 + lane] = tl[rr][lane];
+        __syncwarp();
+    };
+    // pass 1: forward sweep from a zero carry; g = d(d_j)/d(d_{first column - 1})
+    double d = 0.0, g = 1.0;
+    for (int ch = ch_lo; ch < ch_hi; ++ch) {
+        load(src, ch);
+        const int c0 = ch << 5, w = min(32, n1 - c0);
+        double ca = 0.0, ci = 0.0;
+        if (lane < w) { ca = L[vo + c0 + lane]; ci = L[SV + vo + c0 + lane]; }
+        for (int c = 0; c < w; ++c) {
+            const double a = __shfl_sync(FULL, ca, c), inv = __shfl_sync(FULL, ci, c);
+            if (lane < rows) {
+                const int col = c0 + c;
+                double rk = tl[lane][c];
+                if (special) {
+                    d = rk * z;
+                    g = 0.0;
+                } else {
+                    if (col == n1 - 1) rk += 1.0 * rfold * f;
+                    if (col == 0) {
+                        d = rk * inv;
+                        g = 0.0;
+                    } else {
+                        d = (rk - a * d) * inv;
+                        g = (-a * g) * inv;
+                    }
+                }
+                tl[lane][c] = d;
+            }
+        }
+        store(ch);
+    }
+    cval[warp][lane] = d;
+    cwt[warp][lane] = g;
+    __syncthreads();
+    if (warp == 0) {
+        double D = 0.0;   // d at the column before segment s
+        for (int s = 0; s < NSEG; ++s) {
+            const double v = cval[s][lane], wt = cwt[s][lane];
+            cval[s][lane] = D;
+            D = fma(wt, D, v);
+        }
+    }
+    __syncthreads();
+    // pass 2: d_j += g_j * carry (the first segment starts at column 0 and is exact)
+    if (ch_lo > 0) {
+        const double C = cval[warp][lane];
+        double gg = 1.0;
+        for (int ch = ch_lo; ch < ch_hi; ++ch) {
+            load(dst, ch);
+            const int c0 = ch << 5, w = min(32, n1 - c0);
+            double ca = 0.0, ci = 0.0;
+            if (lane < w) { ca = L[vo + c0 + lane]; ci = L[SV + vo + c0 + lane]; }
+            for (int c = 0; c < w; ++c) {
+                const double a = __shfl_sync(FULL, ca, c), inv = __shfl_sync(FULL, ci, c);
+                if (lane < rows) {
+                    gg = special ? 0.0 : (-a * gg) * inv;
+                    tl[lane][c] = fma(gg, C, tl[lane][c]);
+                }
+            }
+            store(ch);
+        }
+    }
+    __syncthreads();
+    // pass 3: back substitution from a zero carry; h = d(x_j)/d(x_{last column + 1})
+    double x = 0.0, h = 1.0;
+    for (int ch = ch_hi - 1; ch >= ch_lo; --ch) {
+        load(dst, ch);
+        const int c0 = ch << 5, w = min(32, n1 - c0);
+        const double cc0 = lane < w ? L[2 * SV + vo + c0 + lane] : 0.0;
+        for (int c = w - 1; c >= 0; --c) {
+            const double cc = __shfl_sync(FULL, cc0, c);
+            if (lane < rows) {
+                const int col = c0 + c;
+                const double dd = tl[lane][c];
+                if (col == n1 - 1 || special) {
+                    x = dd;
+                    h = 0.0;
+                } else {
+                    x = dd - cc * x;
+                    h = -cc * h;
+                }
+                tl[lane][c] = x;
+            }
+        }
+        store(ch);
+    }
+    cval[warp][lane] = x;
+    cwt[warp][lane] = h;
+    __syncthreads();
+    if (warp == 0) {
+        double X = 0.0;   // x at the column after segment s
+        for (int s = NSEG - 1; s >= 0; --s) {
+            const double v = cval[s][lane], wt = cwt[s][lane];
+            cval[s][lane] = X;
+            X = fma(wt, X, v);
+        }
+    }
+    __syncthreads();
+    // pass 4: x_j += h_j * carry (the last segment ends at column n1 - 1 and is exact)
+    if (ch_hi < nch && ch_lo < ch_hi) {
+        const double C = cval[warp][lane];
+        double hh = 1.0;
+        for (int ch = ch_hi - 1; ch >= ch_lo; --ch) {
+            load(dst, ch);
+            const int c0 = ch << 5, w = min(32, n1 - c0);
+            const double cc0 = lane < w ? L[2 * SV + vo + c0 + lane] : 0.0;
+            for (int c = w - 1; c >= 0; --c) {
+                const double cc = __shfl_sync(FULL, cc0, c);
+                if (lane < rows) {
+                    hh = special ? 0.0 : -cc * hh;
+                    tl[lane][c] = fma(hh, C, tl[lane][c]);
+                }
+            }
+            store(ch);
+        }
+    }
+}
+
 // Per-option status: the build's pivot flags, plus FDADI_STATUS_NONFINITE if
 // any value of the option's state grid is NaN or infinite (one block per option).
 __global__ void status_kernel(Arena A, const double *V, int *out) {
@@ -1025,14 +1244,16 @@ static int make_layout(const fdadi_heston_batch_t *b, Layout &L) {
     FDADI_REQUIRE(b != nullptr, "null batch");
     FDADI_REQUIRE(b->n_options > 0, "empty batch");
     FDADI_REQUIRE(b->n0 && b->n1, "batch needs host size arrays n0, n1");
-    FDADI_REQUIRE(b->scheme == FDADI_SCHEME_DOUGLAS || b->scheme == FDADI_SCHEME_HV,
-                  "main scheme must be Douglas or Hundsdorfer-Verwer");
+    FDADI_REQUIRE(b->scheme == FDADI_SCHEME_DOUGLAS || b->scheme == FDADI_SCHEME_HV ||
+                      b->scheme == FDADI_SCHEME_CS || b->scheme == FDADI_SCHEME_MCS,
+                  "main scheme must be Douglas, Hundsdorfer-Verwer or (modified) Craig-Sneyd");
     FDADI_REQUIRE(b->n_steps >= 0 && b->implicit_steps >= 0, "negative step count");
     FDADI_REQUIRE(b->implicit_steps == 0 || b->implicit_dt_factor > 0.0,
                   "implicit_dt_factor must be positive");
     L.n_opt = b->n_options;
     L.smoothing = b->implicit_steps > 0;
-    L.hv = b->scheme == FDADI_SCHEME_HV;
+    // predictor/corrector schemes (HV, CS, MCS) keep F(V) and Y2
+    L.hv = b->scheme != FDADI_SCHEME_DOUGLAS;
     L.p_off.resize(L.n_opt + 1);
     L.s_off.resize(L.n_opt + 1);
     L.v_off.resize(L.n_opt + 1);
@@ -1143,6 +1364,7 @@ struct VarVariant {
     int kind, warps;
     int smem;         // dynamic shared memory bytes
     VarFn main, impl;
+    int tasks;        // tasks per block (kind 3: one task shared by all warps)
 };
 
 #define SPOT_T(PF, TH)                                                                  \
@@ -1162,13 +1384,17 @@ static const SpotVariant SPOT_VARIANTS[] = {
 constexpr int VAR_TILE_BYTES = 32 * VS_PITCH * (int)sizeof(double);
 #define VAR_P(NW, DB)                                                                   \
     VarVariant{DB ? 1 : 2, NW, NW * (DB ? 2 : 1) * VAR_TILE_BYTES,                     \
-               var_solve_pipe_kernel<false, NW, DB>, var_solve_pipe_kernel<true, NW, DB>}
+               var_solve_pipe_kernel<false, NW, DB>, var_solve_pipe_kernel<true, NW, DB>, NW}
+#define VAR_S(NS)                                                                       \
+    VarVariant{3, NS, NS * VAR_TILE_BYTES, var_seg_kernel<false, NS>, var_seg_kernel<true, NS>, 1}
 static const VarVariant VAR_VARIANTS[] = {
-    {0, 4, 0, var_solve_kernel<false, 4>, var_solve_kernel<true, 4>},
-    {0, 2, 0, var_solve_kernel<false, 2>, var_solve_kernel<true, 2>},
+    {0, 4, 0, var_solve_kernel<false, 4>, var_solve_kernel<true, 4>, 4},
+    {0, 2, 0, var_solve_kernel<false, 2>, var_solve_kernel<true, 2>, 2},
     VAR_P(1, true), VAR_P(2, true), VAR_P(4, true),
-    VAR_P(1, false), VAR_P(2, false), VAR_P(4, false)};
+    VAR_P(1, false), VAR_P(2, false), VAR_P(4, false),
+    VAR_S(4), VAR_S(8), VAR_S(16)};
 #undef VAR_P
+#undef VAR_S
 
 constexpr int N_SPOT_VARIANTS = sizeof(SPOT_VARIANTS) / sizeof(SPOT_VARIANTS[0]);
 constexpr int N_VAR_VARIANTS = sizeof(VAR_VARIANTS) / sizeof(VAR_VARIANTS[0]);
@@ -1242,6 +1468,7 @@ struct GroupSpan {
 
 struct Grids {
     int si, vi;       // variant indices
+    int corr;         // explicit mode of the corrector stage (ST_HV3, ST_CS3, ST_MCS3)
     int groups;
     int64_t expl_ctas; // explicit-stage blocks (0: one per tile)
     GroupSpan all;
@@ -1268,6 +1495,7 @@ static int grids(const fdadi_heston_batch_t *b, const Layout &L, Grids &g) {
     FDADI_REQUIRE(p.groups >= 0 && p.groups <= MAX_GROUPS, "plan groups must be 0..%d (%d)",
                   MAX_GROUPS, p.groups);
     g.groups = std::max(1, std::min<int>(p.groups, L.n_opt));
+    g.corr = b->scheme == FDADI_SCHEME_CS ? ST_CS3 : b->scheme == FDADI_SCHEME_MCS ? ST_MCS3 : ST_HV3;
     FDADI_REQUIRE(p.expl_per_sm >= 0 && p.expl_per_sm <= 4,
                   "plan expl_per_sm must be 0..4 (%d)", p.expl_per_sm);
     g.expl_ctas = (int64_t)p.expl_per_sm * sm_count();
@@ -1320,6 +1548,8 @@ static void launch_explicit(int mode, const Span &t, int64_t ctas, const Arena &
     case ST_DOUGLAS: explicit_kernel<ST_DOUGLAS><<<n, EXPL_THREADS, 0, st>>>(A, V, t.lo, t.hi); break;
     case ST_HV0: explicit_kernel<ST_HV0><<<n, EXPL_THREADS, 0, st>>>(A, V, t.lo, t.hi); break;
     case ST_HV3: explicit_kernel<ST_HV3><<<n, EXPL_THREADS, 0, st>>>(A, V, t.lo, t.hi); break;
+    case ST_CS3: explicit_kernel<ST_CS3><<<n, EXPL_THREADS, 0, st>>>(A, V, t.lo, t.hi); break;
+    case ST_MCS3: explicit_kernel<ST_MCS3><<<n, EXPL_THREADS, 0, st>>>(A, V, t.lo, t.hi); break;
     default: explicit_kernel<ST_IMPLICIT><<<n, EXPL_THREADS, 0, st>>>(A, V, t.lo, t.hi); break;
     }
 }
@@ -1332,7 +1562,7 @@ static void launch_spot(int si, bool implicit, const Span &lines, const Arena &A
 static void launch_var(int vi, bool implicit, const Span &tasks, const Arena &A,
                        const double *src, double *dst, cudaStream_t st, int prio) {
     const VarVariant &v = VAR_VARIANTS[vi];
-    const unsigned grid = (unsigned)((tasks.hi - tasks.lo + v.warps - 1) / v.warps);
+    const unsigned grid = (unsigned)((tasks.hi - tasks.lo + v.tasks - 1) / v.tasks);
     launch_ex(implicit ? v.impl : v.main, grid, v.warps * 32, (size_t)v.smem, st, prio, A, tasks,
               src, dst);
 }
@@ -1343,7 +1573,7 @@ static void launch_stage(int stage, const Grids &g, const Arena &A, double *V, c
     switch (stage) {
     case FDADI_STAGE_EXPLICIT_DOUGLAS: launch_explicit(ST_DOUGLAS, a.tiles, g.expl_ctas, A, V, st); break;
     case FDADI_STAGE_EXPLICIT_HV0: launch_explicit(ST_HV0, a.tiles, g.expl_ctas, A, V, st); break;
-    case FDADI_STAGE_EXPLICIT_HV3: launch_explicit(ST_HV3, a.tiles, g.expl_ctas, A, V, st); break;
+    case FDADI_STAGE_EXPLICIT_HV3: launch_explicit(g.corr, a.tiles, g.expl_ctas, A, V, st); break;
     case FDADI_STAGE_EXPLICIT_IMPLICIT: launch_explicit(ST_IMPLICIT, a.tiles, g.expl_ctas, A, V, st); break;
     case FDADI_STAGE_SPOT_SOLVE: launch_spot(g.si, false, a.lines, A, A.W, A.W, st, 0); break;
     case FDADI_STAGE_VAR_SOLVE_TO_Y2: launch_var(g.vi, false, a.tasks, A, A.W, A.Y2, st, 0); break;
@@ -1376,7 +1606,7 @@ static void launch_phase(int kind, const Grids &g, const GroupSpan &s, const Are
         launch_var(g.vi, false, s.tasks, A, A.W, A.Y2, st, prio);
         break;
     default:
-        launch_explicit(ST_HV3, s.tiles, g.expl_ctas, A, V, st);
+        launch_explicit(g.corr, s.tiles, g.expl_ctas, A, V, st);
         launch_spot(g.si, false, s.lines, A, A.W, A.W, st, prio);
         launch_var(g.vi, false, s.tasks, A, A.W, V, st, prio);
         break;
@@ -1446,7 +1676,7 @@ static int launch_steps(const fdadi_heston_batch_t *b, const Layout &L, const Ar
             case PH_IMPLICIT: launch_explicit(ST_IMPLICIT, s.tiles, g.expl_ctas, A, V, sk); break;
             case PH_DOUGLAS: launch_explicit(ST_DOUGLAS, s.tiles, g.expl_ctas, A, V, sk); break;
             case PH_HV_PREDICT: launch_explicit(ST_HV0, s.tiles, g.expl_ctas, A, V, sk); break;
-            default: launch_explicit(ST_HV3, s.tiles, g.expl_ctas, A, V, sk); break;
+            default: launch_explicit(g.corr, s.tiles, g.expl_ctas, A, V, sk); break;
             }
             FDADI_CUDA(cudaEventRecord(chain, sk));
             first = false;
@@ -1528,7 +1758,7 @@ int64_t fdadi_heston_launch_count(const fdadi_heston_batch_t *b) {
     if (b->plan && b->plan->groups > 1)
         groups = std::min<int64_t>(std::min(b->plan->groups, MAX_GROUPS), b->n_options);
     return groups * ((int64_t)3 * b->implicit_steps +
-                     (int64_t)b->n_steps * (b->scheme == FDADI_SCHEME_HV ? 6 : 3));
+                     (int64_t)b->n_steps * (b->scheme == FDADI_SCHEME_DOUGLAS ? 3 : 6));
 }
 
 int fdadi_heston_prepare(const fdadi_heston_batch_t *b, void *workspace, int64_t ws_bytes,
@@ -1637,7 +1867,7 @@ int fdadi_heston_stage(const fdadi_heston_batch_t *b, void *workspace, int64_t w
                   "unknown stage %d", stage);
     FDADI_REQUIRE(!(stage == FDADI_STAGE_EXPLICIT_HV0 || stage == FDADI_STAGE_EXPLICIT_HV3 ||
                     stage == FDADI_STAGE_VAR_SOLVE_TO_Y2) || L.hv,
-                  "stage %d needs a Hundsdorfer-Verwer batch", stage);
+                  "stage %d needs a predictor-corrector (HV or Craig-Sneyd) batch", stage);
     FDADI_REQUIRE(!(stage == FDADI_STAGE_EXPLICIT_IMPLICIT ||
                     stage == FDADI_STAGE_VAR_SOLVE_IMPLICIT ||
                     stage == FDADI_STAGE_SPOT_SOLVE_IMPLICIT) || L.smoothing,
@@ -1739,7 +1969,7 @@ int fdadi_heston_tune(const fdadi_heston_batch_t *b, void *workspace, int64_t ws
     }
     for (int k = 0; k < N_VAR_VARIANTS && !rc; ++k) {
         const VarVariant &v = VAR_VARIANTS[k];
-        const unsigned grid = (unsigned)((L.n_vtasks + v.warps - 1) / v.warps);
+        const unsigned grid = (unsigned)((L.n_vtasks + v.tasks - 1) / v.tasks);
         const Span tasks{0, L.n_vtasks};
         float ms = 0.0f;
         rc = time_it([&] { v.main<<<grid, v.warps * 32, v.smem, st>>>(A, tasks, A.W, A.W); }, ms);

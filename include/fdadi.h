@@ -47,6 +47,8 @@ extern "C" {
 #define FDADI_SCHEME_IMPLICIT 0
 #define FDADI_SCHEME_DOUGLAS 1
 #define FDADI_SCHEME_HV 2
+#define FDADI_SCHEME_CS 3     /* Craig-Sneyd, FiniteDifferenceEngine.pyx:843-898 */
+#define FDADI_SCHEME_MCS 4    /* modified Craig-Sneyd, FiniteDifferenceEngine.pyx:779-841 */
 
 /* library version (major*10000 + minor*100 + patch) */
 int fdadi_version(void);
@@ -167,8 +169,10 @@ typedef struct fdadi_heston_plan {
     int32_t spot_a;      /* kind 0: rows prefetched ahead (1, 2, 4 or 8); kind 1: lines per block */
     int32_t spot_b;      /* kind 0: threads per block; kind 1: segments per line */
     int32_t var_kind;    /* 0: one shared tile per warp; 1: two tiles, copies pipelined,
-                          * factors by shuffle; 2: one tile, factors by shuffle */
-    int32_t var_warps;   /* warps per variance-solve block */
+                          * factors by shuffle; 2: one tile, factors by shuffle;
+                          * 3: partitioned lines (one 32-row task per block, its warps
+                          * splitting the columns) */
+    int32_t var_warps;   /* warps per variance-solve block (kind 3: 4, 8 or 16 segments) */
     int32_t groups;      /* option groups whose explicit stages and solves overlap
                           * (1..4; 0 counts as 1) */
     int32_t expl_per_sm; /* explicit stage: 0 = one block per tile; n = n blocks per SM
@@ -178,7 +182,7 @@ typedef struct fdadi_heston_plan {
 
 typedef struct fdadi_heston_batch {
     int32_t n_options;
-    int32_t scheme;          /* FDADI_SCHEME_DOUGLAS or FDADI_SCHEME_HV (main segment) */
+    int32_t scheme;          /* FDADI_SCHEME_DOUGLAS, _HV, _CS or _MCS (main segment) */
     int32_t n_steps;         /* main-segment steps */
     int32_t implicit_steps;  /* fully implicit steps run before the main segment */
     double theta;            /* main-segment theta */

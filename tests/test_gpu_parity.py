@@ -20,6 +20,8 @@ SCHED = {
     "hv": lambda n, dt: [("hv", n, dt, HV_THETA)],
     "implicit": lambda n, dt: [("implicit", n, dt, 1.0)],
     "smooth": lambda n, dt: [("implicit", 2, dt * 0.5, 1.0), ("hv", n - 1, dt, 0.6)],
+    "cs": lambda n, dt: [("cs", n, dt, 0.5)],
+    "mcs": lambda n, dt: [("mcs", n, dt, 1.0 / 3)],
 }
 BATCH_ARGS = {
     "douglas": lambda n, dt: dict(scheme="douglas", n_steps=n, dt=dt, theta=0.5),
@@ -28,6 +30,8 @@ BATCH_ARGS = {
                                    implicit_steps=n, implicit_dt_factor=1.0),
     "smooth": lambda n, dt: dict(scheme="hv", n_steps=n - 1, dt=dt, theta=0.6,
                                  implicit_steps=2, implicit_dt_factor=0.5),
+    "cs": lambda n, dt: dict(scheme="cs", n_steps=n, dt=dt, theta=0.5),
+    "mcs": lambda n, dt: dict(scheme="mcs", n_steps=n, dt=dt, theta=1.0 / 3),
 }
 
 
@@ -44,7 +48,7 @@ def cuda():
     return torch.device("cuda", 0)
 
 
-@pytest.mark.parametrize("scheme", ["douglas", "hv", "implicit", "smooth"])
+@pytest.mark.parametrize("scheme", ["douglas", "hv", "implicit", "smooth", "cs", "mcs"])
 def test_fused_batch_vs_golden(cuda, golden, scheme):
     """Three parameter sets per scheme in one batch vs the reference outputs."""
     from fd_adi_gb300.batch import HestonBatch

@@ -82,7 +82,7 @@ def test_spot_plan_vs_oracle(uneven, k):
     _check(b.solve(V0), opts, meshes, ref)
 
 
-@pytest.mark.parametrize("k", range(8), ids=lambda k: "var%d" % k)
+@pytest.mark.parametrize("k", range(11), ids=lambda k: "var%d" % k)
 def test_var_plan_vs_oracle(uneven, k):
     from fd_adi_gb300.batch import HestonBatch, SPOT_PLANS, VAR_PLANS, make_plan
     opts, meshes, V0, ref, kw = uneven
@@ -119,7 +119,7 @@ def test_more_groups_than_options(uneven):
 
 def test_plan_list_is_complete(cuda):
     from fd_adi_gb300.batch import SPOT_PLANS, VAR_PLANS
-    assert len(SPOT_PLANS) == 20 and len(VAR_PLANS) == 8
+    assert len(SPOT_PLANS) == 20 and len(VAR_PLANS) == 11
 
 
 def test_unknown_plan_is_rejected(uneven):
@@ -152,8 +152,9 @@ def test_config1_golden_with_plan(cuda, golden, plan):
     assert np.abs(V - g["V"]).max() <= 1e-9 * np.abs(g["V"]).max()
 
 
-def test_config2_golden_partitioned(cuda, golden):
-    """1024x512 (long spot lines: the partitioned solve's case) against the
+@pytest.mark.parametrize("var", [(1, 2), (3, 16), (3, 4)])
+def test_config2_golden_partitioned(cuda, golden, var):
+    """1024x512 (long lines: the partitioned solves' case) against the
     reference's golden output."""
     from fd_adi_gb300.batch import HestonBatch, make_plan
     g = golden("config2_short")
@@ -161,7 +162,7 @@ def test_config2_golden_partitioned(cuda, golden):
     V0 = np.maximum(S[:, None] - 100.0, 0) * np.ones((1, v.size))
     b = HestonBatch([(0.06, 1.0, 0.04, 0.5, -0.7)], [(S, v)], scheme="hv", n_steps=3,
                     dt=1.0 / 1000, theta=HV_THETA, implicit_steps=2, implicit_dt_factor=0.5,
-                    plan=make_plan((1, 8, 128), (1, 2)))
+                    plan=make_plan((1, 8, 128), var))
     V = b.solve([V0])[0]
     idx = tuple(g["idx"])
     assert abs(V[idx] - g["price"]) <= 1e-10 * abs(g["price"])
@@ -253,3 +254,18 @@ def test_greeks_match_host_stencils(uneven):
         # against the oracle's grid: the spec price bar, delta alike
         cr = ref[k][i - 1:i + 2, j]
         assert abs(d[k] - np.dot(w1, cr)) <= 1e-9 * max(1.0, abs(d[k]))
+
+
+@pytest.mark.parametrize("scheme,theta", [("cs", 0.5), ("mcs", 1.0 / 3), ("mcs", 0.8)])
+def test_craig_sneyd_uneven_batch_vs_oracle(uneven, scheme, theta):
+    """Batched Craig-Sneyd / modified Craig-Sneyd after a Rannacher start,
+    uneven grids, with option groups, against the oracle."""
+    from fd_adi_gb300.batch import HestonBatch, SPOT_PLANS, VAR_PLANS, make_plan
+    opts, meshes, V0, ref, kw = uneven
+    dts = kw["dt"]
+    n = 20
+    want = O.heston_batch(meshes, [o.params() for o in opts], V0,
+                          [[("implicit", 2, dt / 2, 1.0), (scheme, n - 1, dt, theta)] for dt in dts])
+    b = HestonBatch(opts, meshes, **dict(kw, scheme=scheme, theta=theta),
+                    plan=make_plan(SPOT_PLANS[0], VAR_PLANS[2], 2))
+    _check(b.solve(V0), opts, meshes, want)
