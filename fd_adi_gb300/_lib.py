@@ -45,6 +45,13 @@ STATUS_PIVOT = 1        # a line-solve pivot was zero or non-finite
 STATUS_NONFINITE = 2    # the option's grid holds a NaN or infinity
 
 
+class MlpNet(ctypes.Structure):
+    """fdadi_mlp_net_t"""
+    _fields_ = [("W", ctypes.c_void_p * 5), ("b", ctypes.c_void_p * 5),
+                ("K", ctypes.c_int32 * 5), ("N", ctypes.c_int32 * 5),
+                ("members", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
 class HestonPlan(ctypes.Structure):
     """fdadi_heston_plan_t"""
     _fields_ = [("spot_kind", ctypes.c_int32), ("spot_a", ctypes.c_int32),
@@ -125,6 +132,8 @@ SIGNATURES = {
                                          ctypes.POINTER(HestonPlan), ctypes.c_void_p]),
     "fdadi_heston_default_plan": (ctypes.c_int, [ctypes.POINTER(HestonBatch),
                                                  ctypes.POINTER(HestonPlan)]),
+    "fdadi_mlp_infer": (ctypes.c_int, [ctypes.POINTER(MlpNet), ctypes.c_void_p, ctypes.c_int32,
+                                       ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "fdadi_heston_greeks": (ctypes.c_int, [ctypes.POINTER(HestonBatch), ctypes.c_void_p,
                                            ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
                                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,

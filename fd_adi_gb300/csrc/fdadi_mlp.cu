@@ -613,6 +613,239 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
     }
 }
 
+// ---- fused surrogate inference (all five layers in one kernel) -------------
+//
+// The ensemble's inference keeps every hidden activation on chip: one CTA per
+// SM loops over (128-query tile, member) units, and per unit runs
+//     X (128 x 16) -> 256 -> 256 -> 256 -> 256 -> first 16 outputs
+// with the accumulator in tensor memory and the 128 x 256 bf16 activation in
+// shared memory, written by the epilogue in the K-major core-matrix layout that
+// the next layer's MMA reads as its A operand. Only the weights stream in (TMA,
+// 32-wide K chunks through a 6-stage ring, L2-resident across units) and only
+// the two outputs per query and member go out. Roles:
+//   warp 0 (one lane): TMA producer for the query tile and the weight chunks,
+//     running ahead across layers;
+//   warp 1: tensor-memory owner; one lane issues each layer's MMAs once the
+//     previous layer's epilogue has released the accumulator and written the
+//     activation, and commits the ring stages, the query tile and the layer;
+//   warps 2-17: epilogue (TMEM lane quarter w % 4, a quarter of the columns each):
+//     bias, SiLU, bf16, st.shared into the activation tile, proxy fence,
+//     arrive; the last layer stores outputs 0 and 1.
+// The layers of one unit are a strict chain, so the tensor pipe idles while
+// the epilogue runs; every wait is bounded and sets the status word.
+constexpr int FI_STAGES = 6;
+constexpr int FI_BK = 32;
+constexpr int FI_EPI_WARPS = 16;
+constexpr int FI_THREADS = 64 + 32 * FI_EPI_WARPS;
+constexpr int FI_X_BYTES = GM_BM * 16 * 2;              // 4 KB query tile
+constexpr int FI_H_BYTES = GM_BM * 256 * 2;             // 64 KB activation
+constexpr int FI_STAGE_BYTES = 256 * FI_BK * 2;         // 16 KB weight chunk
+constexpr int FI_RING = FI_X_BYTES + FI_H_BYTES;
+constexpr int FI_BAR = FI_RING + FI_STAGES * FI_STAGE_BYTES;
+constexpr int FI_SMEM = FI_BAR + 1024;
+constexpr int FI_LAYERS = 5;
+
+struct FiArgs {
+    const float *bias[FI_LAYERS];
+    int64_t bstride[FI_LAYERS];   // bias stride between members
+    float *out;                   // [members][M][2]
+    int M, m_tiles, members;
+    int *status;
+};
+
+__global__ void __launch_bounds__(FI_THREADS, 1)
+    mlp_infer_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tw0,
+                     const __grid_constant__ CUtensorMap tw1, const __grid_constant__ CUtensorMap tw2,
+                     const __grid_constant__ CUtensorMap tw3, const __grid_constant__ CUtensorMap tw4,
+                     FiArgs f) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + FI_BAR);
+    uint64_t *empty = full + FI_STAGES;
+    uint64_t *x_full = empty + FI_STAGES, *x_empty = x_full + 1;
+    uint64_t *acc_full = x_empty + 1, *h_ready = acc_full + 1, *drain = h_ready + 1;
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(drain + 1);
+    volatile int *abort = reinterpret_cast<volatile int *>(tslot + 1);
+    const uint32_t sbase = smem_addr(smem);
+    const uint32_t sx = sbase, sh = sbase + FI_X_BYTES, sring = sbase + FI_RING;
+    const int units = f.m_tiles * f.members;
+    // layer l: K, N of the MMA (the last layer uses its first 16 outputs)
+    const int LK[FI_LAYERS] = {16, 256, 256, 256, 256};
+    const int LN[FI_LAYERS] = {256, 256, 256, 256, 16};
+
+    if (tid == 0) {
+        for (int s = 0; s < FI_STAGES; ++s) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&full[s])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&empty[s])));
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(x_full)));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(x_empty)));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(acc_full)));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(h_ready)),
+                     "r"(FI_EPI_WARPS));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(drain)));
+        *abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     ::"r"(smem_addr(tslot)), "r"(256));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = *tslot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            const CUtensorMap *maps[FI_LAYERS] = {&tw0, &tw1, &tw2, &tw3, &tw4};
+            uint32_t it = 0;
+            int lu = 0;
+            bool ok = true;
+            for (int u = blockIdx.x; u < units && ok; u += gridDim.x, ++lu) {
+                const int mt = u % f.m_tiles, p = u / f.m_tiles;
+                if (lu > 0 && !ws_wait(x_empty, (uint32_t)(lu - 1) & 1, abort)) break;
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                             ::"r"(smem_addr(x_full)), "r"(FI_X_BYTES) : "memory");
+                tma_load_3d(sx, &tmX, 0, mt * GM_BM, 0, x_full);
+                tma_load_3d(sx + GM_BM * 16, &tmX, 8, mt * GM_BM, 0, x_full);
+                for (int l = 0; l < FI_LAYERS && ok; ++l) {
+                    for (int k0 = 0; k0 < LK[l]; k0 += FI_BK, ++it) {
+                        const int s = it % FI_STAGES;
+                        const uint32_t n = it / FI_STAGES;
+                        if (n > 0 && !ws_wait(&empty[s], (n - 1) & 1, abort)) { ok = false; break; }
+                        const int kc = min(FI_BK, LK[l] - k0) >> 3;
+                        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                                     ::"r"(smem_addr(&full[s])), "r"((uint32_t)(kc * LN[l] * 16))
+                                     : "memory");
+                        const uint32_t b0 = sring + s * FI_STAGE_BYTES;
+                        for (int c = 0; c < kc; ++c)
+                            tma_load_3d(b0 + c * LN[l] * 16, maps[l], k0 + 8 * c, 0, p, &full[s]);
+                    }
+                }
+            }
+            // drain, as in the GEMM: copies landed, stages released
+            const uint32_t last = it;
+            for (uint32_t j = last > FI_STAGES ? last - FI_STAGES : 0; j < last; ++j) {
+                const int s = j % FI_STAGES;
+                const uint32_t n = j / FI_STAGES;
+                if (*abort) mbar_wait(&full[s], n & 1);
+                else ws_wait(&empty[s], n & 1, abort);
+            }
+            if (*abort && lu > 0) mbar_wait(x_full, (uint32_t)(lu - 1) & 1);
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            uint32_t it = 0, L = 0;
+            int lu = 0;
+            bool ok = true;
+            for (int u = blockIdx.x; u < units && ok; u += gridDim.x, ++lu) {
+                for (int l = 0; l < FI_LAYERS && ok; ++l, ++L) {
+                    // the previous layer's epilogue has read the accumulator and
+                    // written the activation this layer reads
+                    if (L > 0 && !ws_wait(h_ready, (L - 1) & 1, abort)) { ok = false; break; }
+                    if (l == 0 && !ws_wait(x_full, (uint32_t)lu & 1, abort)) { ok = false; break; }
+                    asm volatile("tcgen05.fence::after_thread_sync;");
+                    const uint32_t idesc = umma_idesc(GM_BM, LN[l]);
+                    const uint32_t abase = l == 0 ? sx : sh;
+                    bool first = true;
+                    for (int k0 = 0; k0 < LK[l]; k0 += FI_BK, ++it) {
+                        const int s = it % FI_STAGES;
+                        const uint32_t n = it / FI_STAGES;
+                        if (!ws_wait(&full[s], n & 1, abort)) { ok = false; break; }
+                        asm volatile("tcgen05.fence::after_thread_sync;");
+                        const int kw = min(FI_BK, LK[l] - k0);
+                        const uint32_t b0 = sring + s * FI_STAGE_BYTES;
+                        for (int q = 0; q < (kw >> 4); ++q) {
+                            const uint64_t ad =
+                                umma_desc(abase + (k0 / 8 + 2 * q) * GM_BM * 16, GM_BM * 16, 128);
+                            const uint64_t bd = umma_desc(b0 + q * 2 * LN[l] * 16, LN[l] * 16, 128);
+                            const uint32_t accum = first ? 0u : 1u;
+                            first = false;
+                            asm volatile(
+                                "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                                "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+                                ::"r"(tmem), "l"(ad), "l"(bd), "r"(idesc), "r"(accum));
+                        }
+                        tcgen05_commit(&empty[s]);
+                    }
+                    if (!ok) break;
+                    if (l == 0) tcgen05_commit(x_empty);
+                    tcgen05_commit(acc_full);
+                }
+            }
+            if (*abort) {
+                tcgen05_commit(drain);
+                mbar_wait(drain, 0);
+            }
+        }
+    } else {
+        // epilogue: warp w -> TMEM lanes 32 (w % 4) ..., column quarter (w - 2) / 4
+        const int q = warp & 3, part = (warp - 2) >> 2;
+        const int row = q * 32 + lane;
+        uint32_t L = 0;
+        bool ok = true;
+        for (int u = blockIdx.x; u < units && ok; u += gridDim.x) {
+            const int mt = u % f.m_tiles, p = u / f.m_tiles;
+            const int m = mt * GM_BM + row;
+            for (int l = 0; l < FI_LAYERS; ++l, ++L) {
+                int w = 1;
+                if (lane == 0) w = ws_wait(acc_full, L & 1, abort) ? 1 : 0;
+                if (!__shfl_sync(0xffffffffu, w, 0)) { ok = false; break; }
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                const float *bias = f.bias[l] + p * f.bstride[l];
+                const int cb = l < FI_LAYERS - 1 ? part * 64 : 0;
+                const int ce = l < FI_LAYERS - 1 ? cb + 64 : (part == 0 ? 8 : 0);
+                for (int c0 = cb; c0 < ce; c0 += 8) {
+                    uint32_t r[8];
+                    const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0;
+                    asm volatile(
+                        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+                          "=r"(r[6]), "=r"(r[7])
+                        : "r"(taddr));
+                    const float4 b0 = *reinterpret_cast<const float4 *>(bias + c0);
+                    const float4 b1 = *reinterpret_cast<const float4 *>(bias + c0 + 4);
+                    asm volatile("tcgen05.wait::ld.sync.aligned;");
+                    const float bb[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+                    float x[8];
+#pragma unroll
+                    for (int e = 0; e < 8; ++e) x[e] = __uint_as_float(r[e]) + bb[e];
+                    if (l == FI_LAYERS - 1) {
+                        *reinterpret_cast<float2 *>(f.out + ((int64_t)p * f.M + m) * 2) =
+                            make_float2(x[0], x[1]);
+                    } else {
+                        __align__(16) bf16 h[8];
+#pragma unroll
+                        for (int e = 0; e < 8; ++e)
+                            h[e] = __float2bfloat16(__fdividef(x[e], 1.0f + __expf(-x[e])));
+                        const uint4 hv = *reinterpret_cast<const uint4 *>(h);
+                        asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};"
+                                     ::"r"(sh + (c0 / 8) * GM_BM * 16 + row * 16), "r"(hv.x),
+                                       "r"(hv.y), "r"(hv.z), "r"(hv.w) : "memory");
+                    }
+                }
+                // the activation is read by the tensor core (async proxy)
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                asm volatile("tcgen05.fence::before_thread_sync;");
+                __syncwarp();
+                if (lane == 0)
+                    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];"
+                                 ::"r"(smem_addr(h_ready)) : "memory");
+            }
+        }
+    }
+    __syncthreads();
+    if (*abort) {
+        if (tid == 0 && f.status) atomicExch(f.status, 1);
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(256));
+    }
+}
+
 // out[c][r] = in[r][c] for an R x C bf16 matrix (per problem: blockIdx.z).
 __global__ void transpose_bf16_kernel(const bf16 *in, int64_t ldi, int64_t stride_in, bf16 *out,
                                       int64_t ldo, int64_t stride_out, int R, int C) {
@@ -888,6 +1121,58 @@ static int launch_ws(const fdadi_gemm_t *a, const GemmArgs &g, cudaStream_t st) 
     const int units = w.m_tiles * w.ksplit * w.problems;
     const unsigned grid = (unsigned)std::min(units, sms);
     umma_gemm_ws_kernel<<<grid, WS_THREADS, WS_SMEM, st>>>(mA, mB, mY, mH, w);
+    FDADI_CHECK_LAUNCH();
+    return FDADI_OK;
+}
+
+int fdadi_mlp_infer(const fdadi_mlp_net_t *net, const void *X, int32_t M, float *out,
+                    int32_t *status, void *stream) {
+    FDADI_REQUIRE(net && X && out, "null inference argument");
+    FDADI_REQUIRE(M > 0 && M % 128 == 0, "inference M must be a positive multiple of 128 (%d)", M);
+    FDADI_REQUIRE(net->members >= 1, "inference needs at least one member");
+    static const int K[FI_LAYERS] = {16, 256, 256, 256, 256};
+    for (int l = 0; l < FI_LAYERS; ++l) {
+        FDADI_REQUIRE(net->W[l] && net->b[l], "null weights or bias of layer %d", l);
+        FDADI_REQUIRE(net->K[l] == K[l], "layer %d must have K = %d (%d)", l, K[l], net->K[l]);
+        FDADI_REQUIRE(l < FI_LAYERS - 1 ? net->N[l] == 256 : (net->N[l] >= 16 && net->N[l] <= 256),
+                      "layer %d width %d not supported (hidden 256, last 16..256)", l, net->N[l]);
+        FDADI_REQUIRE((uintptr_t)net->W[l] % 16 == 0 && (uintptr_t)net->b[l] % 16 == 0 &&
+                          net->N[l] % 4 == 0,
+                      "layer %d weights and bias must be 16-byte aligned", l);
+    }
+    FDADI_REQUIRE((uintptr_t)X % 16 == 0 && (uintptr_t)out % 8 == 0, "misaligned input or output");
+    static bool attr[64] = {false};
+    int dev = 0;
+    FDADI_CUDA(cudaGetDevice(&dev));
+    FDADI_REQUIRE(dev >= 0 && dev < 64, "device ordinal out of range");
+    if (!attr[dev]) {
+        FDADI_CUDA(cudaFuncSetAttribute(mlp_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        FI_SMEM));
+        attr[dev] = true;
+    }
+    CUtensorMap mX, mW[FI_LAYERS];
+    int rc = make_operand_map(&mX, X, M, 16, 16, 0, 1, GM_BM);
+    if (rc) return rc;
+    for (int l = 0; l < FI_LAYERS; ++l) {
+        rc = make_operand_map(&mW[l], net->W[l], net->N[l], K[l], K[l],
+                              (int64_t)net->N[l] * K[l], net->members,
+                              l < FI_LAYERS - 1 ? 256 : 16);
+        if (rc) return rc;
+    }
+    FiArgs f;
+    for (int l = 0; l < FI_LAYERS; ++l) {
+        f.bias[l] = net->b[l];
+        f.bstride[l] = net->N[l];
+    }
+    f.out = out;
+    f.M = M;
+    f.m_tiles = M / GM_BM;
+    f.members = net->members;
+    f.status = status;
+    const int units = f.m_tiles * f.members;
+    const unsigned grid = (unsigned)std::min(units, sm_count());
+    mlp_infer_kernel<<<grid, FI_THREADS, FI_SMEM, as_stream(stream)>>>(mX, mW[0], mW[1], mW[2],
+                                                                      mW[3], mW[4], f);
     FDADI_CHECK_LAUNCH();
     return FDADI_OK;
 }

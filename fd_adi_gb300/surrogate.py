@@ -123,6 +123,22 @@ class MLPEnsemble(object):
                 A, lda, sA = b["H"][li], N, M * N
         return b["Y"][-1]
 
+    def infer(self, X, M, out=None):
+        """Inference in one fused kernel (activations stay on chip): fp32
+        [P][M][2], the network's two scaled residual outputs."""
+        if out is None:
+            out = torch.empty(self.P, M, 2, dtype=torch.float32, device=self.dev)
+        net = _lib.MlpNet()
+        for li, (K, N) in enumerate(LAYERS):
+            net.W[li] = self.Wb[li].data_ptr()
+            net.b[li] = self.b[li].data_ptr()
+            net.K[li] = K
+            net.N[li] = N
+        net.members = self.P
+        _lib.call("fdadi_mlp_infer", ctypes.byref(net), _p(X), int(M), _p(out),
+                  _p(self.status), _st())
+        return out
+
     # -- one training step --
     def train_step(self, X, target, M, lr):
         """X bf16 [M][16], target fp32 [M][2]."""
@@ -296,14 +312,14 @@ class Surrogate(object):
         if M != M0:
             Q = torch.cat([Q, Q[-1:].expand(M - M0, 9)], 0)
         X, base, inbox = self.feat(Q)
-        Y = self.net.forward(X, M, keep_preact=False)
+        Y = self.net.infer(X, M)
         d = self.dev
         price = torch.empty(M, dtype=torch.float64, device=d)
         delta = torch.empty(M, dtype=torch.float64, device=d)
         spread = torch.empty(M, dtype=torch.float64, device=d)
         fb = torch.empty(M, dtype=torch.int32, device=d)
         cnt = torch.zeros(1, dtype=torch.int32, device=d)
-        _lib.call("fdadi_mlp_combine", _p(Y), 128, M * 128, self.net.P, M, _p(Q), _p(base),
+        _lib.call("fdadi_mlp_combine", _p(Y), 2, M * 2, self.net.P, M, _p(Q), _p(base),
                   _p(inbox), float(self.s[0]), float(self.s[1]), float(self.tol), _p(price),
                   _p(delta), _p(spread), _p(fb), _p(cnt), _st())
         return price[:M0], delta[:M0], spread[:M0], fb[:M0], cnt

@@ -316,6 +316,27 @@ typedef struct fdadi_gemm {
 } fdadi_gemm_t;
 int fdadi_mlp_gemm(const fdadi_gemm_t *gemm, void *stream);
 
+/* The surrogate network for fused inference: per layer l, weights W[l] (bf16
+ * [members][N[l]][K[l]], K contiguous) and bias b[l] (fp32 [members][N[l]]).
+ * Supported shape: K = 16, 256, 256, 256, 256; N = 256 for the hidden layers,
+ * 16..256 for the last (its first two outputs are produced). */
+typedef struct fdadi_mlp_net {
+    const void *W[5];
+    const float *b[5];
+    int32_t K[5], N[5];
+    int32_t members;
+    int32_t reserved;
+} fdadi_mlp_net_t;
+
+/* Ensemble inference with every hidden activation kept on chip: one
+ * persistent kernel runs all five layers (tcgen05 MMAs into tensor memory,
+ * bias + SiLU epilogue writing the next layer's bf16 operand in shared memory,
+ * weights streamed by TMA). X: bf16 [M][16] shared by the members, M a
+ * multiple of 128; out: fp32 [members][M][2] (the last layer's first two
+ * outputs, bias included). status: set to 1 if a bounded wait timed out. */
+int fdadi_mlp_infer(const fdadi_mlp_net_t *net, const void *X, int32_t M, float *out,
+                    int32_t *status, void *stream);
+
 /* out[c][r] = in[r][c] (bf16), per problem. */
 int fdadi_transpose_bf16(const void *in, int64_t ldi, int64_t stride_in, void *out, int64_t ldo,
                          int64_t stride_out, int32_t rows, int32_t cols, int32_t problems,

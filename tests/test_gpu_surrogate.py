@@ -119,3 +119,28 @@ def test_surrogate_learns_adi_prices_and_gates(dev):
     torch.cuda.synchronize()
     t_sur = (time.perf_counter() - t0) / Qbig.shape[0]
     assert t_sur * 100 < t_adi
+
+
+def test_fused_inference_matches_layered_forward(dev):
+    """The one-kernel inference against the layer-by-layer tensor-core forward
+    on the same bf16 weights: both round activations to bf16 at the same
+    points, so they agree to accumulation order (1e-3 of the output scale)."""
+    from fd_adi_gb300.surrogate import MLPEnsemble
+    M = 128 * 200              # more tiles than SMs: every CTA loops over units
+    net = MLPEnsemble(members=4, seed=5, device=dev)
+    g = torch.Generator(device="cpu").manual_seed(2)
+    for li in range(len(net.b)):
+        net.b[li].copy_(torch.randn(net.b[li].shape, generator=g) * 0.1)
+    X = torch.zeros(M, 16)
+    X[:, :14] = torch.rand(M, 14, generator=g) * 2 - 1
+    X = X.to(torch.bfloat16).to(dev)
+    ref = net.forward(X, M, keep_preact=False)[:, :, :2].clone()
+    out = net.infer(X, M)
+    torch.cuda.synchronize()
+    net.check()
+    scale = ref.abs().max().item()
+    assert scale > 0
+    assert (out - ref).abs().max().item() <= 1e-3 * scale
+    again = net.infer(X, M)
+    torch.cuda.synchronize()
+    assert torch.equal(again, out)
