@@ -76,6 +76,12 @@ __device__ __forceinline__ uint32_t umma_idesc(int M, int N) {
 }
 
 __device__ __forceinline__ float silu(float x) { return x / (1.0f + expf(-x)); }
+
+// SiLU and the logistic sigmoid with the fast exponential and division
+// intrinsics (the epilogues of the warp-specialised GEMM and of the fused
+// inference use the same forms, so the two inference paths agree).
+__device__ __forceinline__ float silu_fast(float x) { return __fdividef(x, 1.0f + __expf(-x)); }
+__device__ __forceinline__ float sigmoid_fast(float x) { return __fdividef(1.0f, 1.0f + __expf(-x)); }
 __device__ __forceinline__ float dsilu(float x) {
     const float s = 1.0f / (1.0f + expf(-x));
     return s * (1.0f + x * (1.0f - s));
@@ -545,19 +551,21 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
                                 a8[0] = a0.x; a8[1] = a0.y; a8[2] = a0.z; a8[3] = a0.w;
                                 a8[4] = a1.x; a8[5] = a1.y; a8[6] = a1.z; a8[7] = a1.w;
                             }
-                            __align__(16) bf16 h[8];
+                            float y[8];
 #pragma unroll
                             for (int e = 0; e < 8; ++e) {
-                                float y = x[e];
+                                y[e] = x[e];
                                 if (g.act == 1) {
-                                    y = __fdividef(y, 1.0f + __expf(-y));
+                                    y[e] = silu_fast(x[e]);
                                 } else if (g.act == 2) {
-                                    const float sg = __fdividef(1.0f, 1.0f + __expf(-a8[e]));
-                                    y *= sg * (1.0f + a8[e] * (1.0f - sg));
+                                    const float sg = sigmoid_fast(a8[e]);
+                                    y[e] *= sg * (1.0f + a8[e] * (1.0f - sg));
                                 }
-                                h[e] = __float2bfloat16(y);
                             }
-                            const uint4 hv = *reinterpret_cast<const uint4 *>(h);
+                            __align__(16) __nv_bfloat162 h2[4];
+#pragma unroll
+                            for (int e = 0; e < 4; ++e) h2[e] = __floats2bfloat162_rn(y[2 * e], y[2 * e + 1]);
+                            const uint4 hv = *reinterpret_cast<const uint4 *>(h2);
                             const uint32_t lo = (uint32_t)(lane * rh + (g8 / 8) * 16);
                             const uint32_t ph = lo ^ (((lo >> 7) & (uint32_t)(rh / 16 - 1)) << 4);
                             asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};"
@@ -621,26 +629,30 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
 // with the accumulator in tensor memory and the 128 x 256 bf16 activation in
 // shared memory, written by the epilogue in the K-major core-matrix layout that
 // the next layer's MMA reads as its A operand. Only the weights stream in (TMA,
-// 32-wide K chunks through a 6-stage ring, L2-resident across units) and only
-// the two outputs per query and member go out. Roles:
-//   warp 0 (one lane): TMA producer for the query tile and the weight chunks,
-//     running ahead across layers;
-//   warp 1: tensor-memory owner; one lane issues each layer's MMAs once the
-//     previous layer's epilogue has released the accumulator and written the
-//     activation, and commits the ring stages, the query tile and the layer;
-//   warps 2-17: epilogue (TMEM lane quarter w % 4, a quarter of the columns each):
-//     bias, SiLU, bf16, st.shared into the activation tile, proxy fence,
-//     arrive; the last layer stores outputs 0 and 1.
-// The layers of one unit are a strict chain, so the tensor pipe idles while
-// the epilogue runs; every wait is bounded and sets the status word.
-constexpr int FI_STAGES = 6;
+// 32-wide K chunks through a ring, L2-resident across units) and only the two
+// outputs per query and member go out. The layers of one unit form a strict
+// chain, so each CTA keeps two units in flight (slots 0 and 1, each with its
+// own query tile, activation tile and 256-column accumulator) and interleaves
+// them layer by layer: the epilogue of one slot runs while the MMAs of the
+// other do. Roles:
+//   warp 0 (one lane): TMA producer for the query tiles and the weight chunks,
+//     in the order the MMAs consume them, running ahead across layers;
+//   warp 1: tensor-memory owner; one lane issues each (layer, slot)'s MMAs once
+//     that slot's previous epilogue has released the accumulator and written
+//     the activation, and commits the ring stages, the query tile and the layer;
+//   warps 2-17: epilogue (TMEM lane quarter w % 4, a quarter of the columns
+//     each): bias, SiLU, bf16, st.shared into the slot's activation tile,
+//     proxy fence, arrive; the last layer stores outputs 0 and 1.
+// Every wait is bounded and sets the status word.
+constexpr int FI_STAGES = 5;
 constexpr int FI_BK = 32;
 constexpr int FI_EPI_WARPS = 16;
 constexpr int FI_THREADS = 64 + 32 * FI_EPI_WARPS;
 constexpr int FI_X_BYTES = GM_BM * 16 * 2;              // 4 KB query tile
 constexpr int FI_H_BYTES = GM_BM * 256 * 2;             // 64 KB activation
 constexpr int FI_STAGE_BYTES = 256 * FI_BK * 2;         // 16 KB weight chunk
-constexpr int FI_RING = FI_X_BYTES + FI_H_BYTES;
+constexpr int FI_H = 2 * FI_X_BYTES;                    // activations after both query tiles
+constexpr int FI_RING = FI_H + 2 * FI_H_BYTES;
 constexpr int FI_BAR = FI_RING + FI_STAGES * FI_STAGE_BYTES;
 constexpr int FI_SMEM = FI_BAR + 1024;
 constexpr int FI_LAYERS = 5;
@@ -662,13 +674,18 @@ __global__ void __launch_bounds__(FI_THREADS, 1)
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     uint64_t *full = reinterpret_cast<uint64_t *>(smem + FI_BAR);
     uint64_t *empty = full + FI_STAGES;
-    uint64_t *x_full = empty + FI_STAGES, *x_empty = x_full + 1;
-    uint64_t *acc_full = x_empty + 1, *h_ready = acc_full + 1, *drain = h_ready + 1;
+    uint64_t *x_full = empty + FI_STAGES, *x_empty = x_full + 2;    // [2] per slot
+    uint64_t *acc_full = x_empty + 2, *h_ready = acc_full + 2;      // [2] per slot
+    uint64_t *drain = h_ready + 2;
     uint32_t *tslot = reinterpret_cast<uint32_t *>(drain + 1);
     volatile int *abort = reinterpret_cast<volatile int *>(tslot + 1);
     const uint32_t sbase = smem_addr(smem);
-    const uint32_t sx = sbase, sh = sbase + FI_X_BYTES, sring = sbase + FI_RING;
+    const uint32_t sring = sbase + FI_RING;
     const int units = f.m_tiles * f.members;
+    // unit k of this CTA is blockIdx.x + k * gridDim.x, in slot k % 2; pair j
+    // holds units 2j and 2j + 1
+    const int nmine = units > (int)blockIdx.x ? (units - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    const int npairs = (nmine + 1) / 2;
     // layer l: K, N of the MMA (the last layer uses its first 16 outputs)
     const int LK[FI_LAYERS] = {16, 256, 256, 256, 256};
     const int LN[FI_LAYERS] = {256, 256, 256, 256, 16};
@@ -678,18 +695,20 @@ __global__ void __launch_bounds__(FI_THREADS, 1)
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&full[s])));
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&empty[s])));
         }
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(x_full)));
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(x_empty)));
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(acc_full)));
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(h_ready)),
-                     "r"(FI_EPI_WARPS));
+        for (int z = 0; z < 2; ++z) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&x_full[z])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&x_empty[z])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&acc_full[z])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&h_ready[z])),
+                         "r"(FI_EPI_WARPS));
+        }
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(drain)));
         *abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;");
     }
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
-                     ::"r"(smem_addr(tslot)), "r"(256));
+                     ::"r"(smem_addr(tslot)), "r"(512));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
@@ -701,78 +720,96 @@ __global__ void __launch_bounds__(FI_THREADS, 1)
         if (lane == 0) {
             const CUtensorMap *maps[FI_LAYERS] = {&tw0, &tw1, &tw2, &tw3, &tw4};
             uint32_t it = 0;
-            int lu = 0;
             bool ok = true;
-            for (int u = blockIdx.x; u < units && ok; u += gridDim.x, ++lu) {
-                const int mt = u % f.m_tiles, p = u / f.m_tiles;
-                if (lu > 0 && !ws_wait(x_empty, (uint32_t)(lu - 1) & 1, abort)) break;
-                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
-                             ::"r"(smem_addr(x_full)), "r"(FI_X_BYTES) : "memory");
-                tma_load_3d(sx, &tmX, 0, mt * GM_BM, 0, x_full);
-                tma_load_3d(sx + GM_BM * 16, &tmX, 8, mt * GM_BM, 0, x_full);
+            for (int j = 0; j < npairs && ok; ++j) {
+                const int nz = min(2, nmine - 2 * j);
+                for (int z = 0; z < nz; ++z) {
+                    const int u = blockIdx.x + (2 * j + z) * gridDim.x;
+                    const int mt = u % f.m_tiles;
+                    if (j > 0 && !ws_wait(&x_empty[z], (uint32_t)(j - 1) & 1, abort)) { ok = false; break; }
+                    const uint32_t sx = sbase + z * FI_X_BYTES;
+                    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                                 ::"r"(smem_addr(&x_full[z])), "r"(FI_X_BYTES) : "memory");
+                    tma_load_3d(sx, &tmX, 0, mt * GM_BM, 0, &x_full[z]);
+                    tma_load_3d(sx + GM_BM * 16, &tmX, 8, mt * GM_BM, 0, &x_full[z]);
+                }
                 for (int l = 0; l < FI_LAYERS && ok; ++l) {
-                    for (int k0 = 0; k0 < LK[l]; k0 += FI_BK, ++it) {
-                        const int s = it % FI_STAGES;
-                        const uint32_t n = it / FI_STAGES;
-                        if (n > 0 && !ws_wait(&empty[s], (n - 1) & 1, abort)) { ok = false; break; }
-                        const int kc = min(FI_BK, LK[l] - k0) >> 3;
-                        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
-                                     ::"r"(smem_addr(&full[s])), "r"((uint32_t)(kc * LN[l] * 16))
-                                     : "memory");
-                        const uint32_t b0 = sring + s * FI_STAGE_BYTES;
-                        for (int c = 0; c < kc; ++c)
-                            tma_load_3d(b0 + c * LN[l] * 16, maps[l], k0 + 8 * c, 0, p, &full[s]);
+                    for (int z = 0; z < nz && ok; ++z) {
+                        const int p = (int)((blockIdx.x + (2 * j + z) * gridDim.x) / f.m_tiles);
+                        for (int k0 = 0; k0 < LK[l]; k0 += FI_BK, ++it) {
+                            const int s = it % FI_STAGES;
+                            const uint32_t n = it / FI_STAGES;
+                            if (n > 0 && !ws_wait(&empty[s], (n - 1) & 1, abort)) { ok = false; break; }
+                            const int kc = min(FI_BK, LK[l] - k0) >> 3;
+                            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                                         ::"r"(smem_addr(&full[s])), "r"((uint32_t)(kc * LN[l] * 16))
+                                         : "memory");
+                            const uint32_t b0 = sring + s * FI_STAGE_BYTES;
+                            for (int c = 0; c < kc; ++c)
+                                tma_load_3d(b0 + c * LN[l] * 16, maps[l], k0 + 8 * c, 0, p, &full[s]);
+                        }
                     }
                 }
             }
             // drain, as in the GEMM: copies landed, stages released
             const uint32_t last = it;
-            for (uint32_t j = last > FI_STAGES ? last - FI_STAGES : 0; j < last; ++j) {
-                const int s = j % FI_STAGES;
-                const uint32_t n = j / FI_STAGES;
+            for (uint32_t q = last > FI_STAGES ? last - FI_STAGES : 0; q < last; ++q) {
+                const int s = q % FI_STAGES;
+                const uint32_t n = q / FI_STAGES;
                 if (*abort) mbar_wait(&full[s], n & 1);
                 else ws_wait(&empty[s], n & 1, abort);
             }
-            if (*abort && lu > 0) mbar_wait(x_full, (uint32_t)(lu - 1) & 1);
+            if (*abort) {
+                // the last query tile of each slot
+                for (int z = 0; z < 2; ++z) {
+                    const int cnt = (nmine - z + 1) / 2;   // tiles loaded into slot z (at most)
+                    if (cnt > 0) mbar_wait(&x_full[z], (uint32_t)(cnt - 1) & 1);
+                }
+            }
         }
     } else if (warp == 1) {
         if (lane == 0) {
-            uint32_t it = 0, L = 0;
-            int lu = 0;
+            uint32_t it = 0;
             bool ok = true;
-            for (int u = blockIdx.x; u < units && ok; u += gridDim.x, ++lu) {
-                for (int l = 0; l < FI_LAYERS && ok; ++l, ++L) {
-                    // the previous layer's epilogue has read the accumulator and
-                    // written the activation this layer reads
-                    if (L > 0 && !ws_wait(h_ready, (L - 1) & 1, abort)) { ok = false; break; }
-                    if (l == 0 && !ws_wait(x_full, (uint32_t)lu & 1, abort)) { ok = false; break; }
-                    asm volatile("tcgen05.fence::after_thread_sync;");
-                    const uint32_t idesc = umma_idesc(GM_BM, LN[l]);
-                    const uint32_t abase = l == 0 ? sx : sh;
-                    bool first = true;
-                    for (int k0 = 0; k0 < LK[l]; k0 += FI_BK, ++it) {
-                        const int s = it % FI_STAGES;
-                        const uint32_t n = it / FI_STAGES;
-                        if (!ws_wait(&full[s], n & 1, abort)) { ok = false; break; }
+            for (int j = 0; j < npairs && ok; ++j) {
+                const int nz = min(2, nmine - 2 * j);
+                for (int l = 0; l < FI_LAYERS && ok; ++l) {
+                    for (int z = 0; z < nz && ok; ++z) {
+                        // this slot's previous epilogue has read its accumulator
+                        // and written the activation this layer reads
+                        const uint32_t Lz = (uint32_t)(j * FI_LAYERS + l);
+                        if (Lz > 0 && !ws_wait(&h_ready[z], (Lz - 1) & 1, abort)) { ok = false; break; }
+                        if (l == 0 && !ws_wait(&x_full[z], (uint32_t)j & 1, abort)) { ok = false; break; }
                         asm volatile("tcgen05.fence::after_thread_sync;");
-                        const int kw = min(FI_BK, LK[l] - k0);
-                        const uint32_t b0 = sring + s * FI_STAGE_BYTES;
-                        for (int q = 0; q < (kw >> 4); ++q) {
-                            const uint64_t ad =
-                                umma_desc(abase + (k0 / 8 + 2 * q) * GM_BM * 16, GM_BM * 16, 128);
-                            const uint64_t bd = umma_desc(b0 + q * 2 * LN[l] * 16, LN[l] * 16, 128);
-                            const uint32_t accum = first ? 0u : 1u;
-                            first = false;
-                            asm volatile(
-                                "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-                                "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
-                                ::"r"(tmem), "l"(ad), "l"(bd), "r"(idesc), "r"(accum));
+                        const uint32_t idesc = umma_idesc(GM_BM, LN[l]);
+                        const uint32_t abase = l == 0 ? sbase + z * FI_X_BYTES
+                                                      : sbase + FI_H + z * FI_H_BYTES;
+                        const uint32_t d = tmem + (uint32_t)(z * 256);
+                        bool first = true;
+                        for (int k0 = 0; k0 < LK[l]; k0 += FI_BK, ++it) {
+                            const int s = it % FI_STAGES;
+                            const uint32_t n = it / FI_STAGES;
+                            if (!ws_wait(&full[s], n & 1, abort)) { ok = false; break; }
+                            asm volatile("tcgen05.fence::after_thread_sync;");
+                            const int kw = min(FI_BK, LK[l] - k0);
+                            const uint32_t b0 = sring + s * FI_STAGE_BYTES;
+                            for (int q = 0; q < (kw >> 4); ++q) {
+                                const uint64_t ad = umma_desc(abase + (k0 / 8 + 2 * q) * GM_BM * 16,
+                                                              GM_BM * 16, 128);
+                                const uint64_t bd = umma_desc(b0 + q * 2 * LN[l] * 16, LN[l] * 16, 128);
+                                const uint32_t accum = first ? 0u : 1u;
+                                first = false;
+                                asm volatile(
+                                    "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+                                    ::"r"(d), "l"(ad), "l"(bd), "r"(idesc), "r"(accum));
+                            }
+                            tcgen05_commit(&empty[s]);
                         }
-                        tcgen05_commit(&empty[s]);
+                        if (!ok) break;
+                        if (l == 0) tcgen05_commit(&x_empty[z]);
+                        tcgen05_commit(&acc_full[z]);
                     }
-                    if (!ok) break;
-                    if (l == 0) tcgen05_commit(x_empty);
-                    tcgen05_commit(acc_full);
                 }
             }
             if (*abort) {
@@ -784,55 +821,61 @@ __global__ void __launch_bounds__(FI_THREADS, 1)
         // epilogue: warp w -> TMEM lanes 32 (w % 4) ..., column quarter (w - 2) / 4
         const int q = warp & 3, part = (warp - 2) >> 2;
         const int row = q * 32 + lane;
-        uint32_t L = 0;
         bool ok = true;
-        for (int u = blockIdx.x; u < units && ok; u += gridDim.x) {
-            const int mt = u % f.m_tiles, p = u / f.m_tiles;
-            const int m = mt * GM_BM + row;
-            for (int l = 0; l < FI_LAYERS; ++l, ++L) {
-                int w = 1;
-                if (lane == 0) w = ws_wait(acc_full, L & 1, abort) ? 1 : 0;
-                if (!__shfl_sync(0xffffffffu, w, 0)) { ok = false; break; }
-                asm volatile("tcgen05.fence::after_thread_sync;");
-                const float *bias = f.bias[l] + p * f.bstride[l];
-                const int cb = l < FI_LAYERS - 1 ? part * 64 : 0;
-                const int ce = l < FI_LAYERS - 1 ? cb + 64 : (part == 0 ? 8 : 0);
-                for (int c0 = cb; c0 < ce; c0 += 8) {
-                    uint32_t r[8];
-                    const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0;
-                    asm volatile(
-                        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
-                        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
-                          "=r"(r[6]), "=r"(r[7])
-                        : "r"(taddr));
-                    const float4 b0 = *reinterpret_cast<const float4 *>(bias + c0);
-                    const float4 b1 = *reinterpret_cast<const float4 *>(bias + c0 + 4);
-                    asm volatile("tcgen05.wait::ld.sync.aligned;");
-                    const float bb[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
-                    float x[8];
+        for (int j = 0; j < npairs && ok; ++j) {
+            const int nz = min(2, nmine - 2 * j);
+            for (int l = 0; l < FI_LAYERS && ok; ++l) {
+                for (int z = 0; z < nz; ++z) {
+                    const int u = blockIdx.x + (2 * j + z) * gridDim.x;
+                    const int mt = u % f.m_tiles, p = u / f.m_tiles;
+                    const int m = mt * GM_BM + row;
+                    const uint32_t Lz = (uint32_t)(j * FI_LAYERS + l);
+                    int w = 1;
+                    if (lane == 0) w = ws_wait(&acc_full[z], Lz & 1, abort) ? 1 : 0;
+                    if (!__shfl_sync(0xffffffffu, w, 0)) { ok = false; break; }
+                    asm volatile("tcgen05.fence::after_thread_sync;");
+                    const float *bias = f.bias[l] + p * f.bstride[l];
+                    const uint32_t shz = sbase + FI_H + z * FI_H_BYTES;
+                    const int cb = l < FI_LAYERS - 1 ? part * 64 : 0;
+                    const int ce = l < FI_LAYERS - 1 ? cb + 64 : (part == 0 ? 8 : 0);
+                    for (int c0 = cb; c0 < ce; c0 += 8) {
+                        uint32_t r[8];
+                        const uint32_t taddr =
+                            tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(z * 256 + c0);
+                        asm volatile(
+                            "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+                              "=r"(r[6]), "=r"(r[7])
+                            : "r"(taddr));
+                        const float4 b0 = *reinterpret_cast<const float4 *>(bias + c0);
+                        const float4 b1 = *reinterpret_cast<const float4 *>(bias + c0 + 4);
+                        asm volatile("tcgen05.wait::ld.sync.aligned;");
+                        const float bb[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+                        float x[8];
 #pragma unroll
-                    for (int e = 0; e < 8; ++e) x[e] = __uint_as_float(r[e]) + bb[e];
-                    if (l == FI_LAYERS - 1) {
-                        *reinterpret_cast<float2 *>(f.out + ((int64_t)p * f.M + m) * 2) =
-                            make_float2(x[0], x[1]);
-                    } else {
-                        __align__(16) bf16 h[8];
+                        for (int e = 0; e < 8; ++e) x[e] = __uint_as_float(r[e]) + bb[e];
+                        if (l == FI_LAYERS - 1) {
+                            *reinterpret_cast<float2 *>(f.out + ((int64_t)p * f.M + m) * 2) =
+                                make_float2(x[0], x[1]);
+                        } else {
+                            __align__(16) __nv_bfloat162 h2[4];
 #pragma unroll
-                        for (int e = 0; e < 8; ++e)
-                            h[e] = __float2bfloat16(__fdividef(x[e], 1.0f + __expf(-x[e])));
-                        const uint4 hv = *reinterpret_cast<const uint4 *>(h);
-                        asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};"
-                                     ::"r"(sh + (c0 / 8) * GM_BM * 16 + row * 16), "r"(hv.x),
-                                       "r"(hv.y), "r"(hv.z), "r"(hv.w) : "memory");
+                            for (int e = 0; e < 4; ++e)
+                                h2[e] = __floats2bfloat162_rn(silu_fast(x[2 * e]), silu_fast(x[2 * e + 1]));
+                            const uint4 hv = *reinterpret_cast<const uint4 *>(h2);
+                            asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};"
+                                         ::"r"(shz + (c0 / 8) * GM_BM * 16 + row * 16), "r"(hv.x),
+                                           "r"(hv.y), "r"(hv.z), "r"(hv.w) : "memory");
+                        }
                     }
+                    // the activation is read by the tensor core (async proxy)
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    asm volatile("tcgen05.fence::before_thread_sync;");
+                    __syncwarp();
+                    if (lane == 0)
+                        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];"
+                                     ::"r"(smem_addr(&h_ready[z])) : "memory");
                 }
-                // the activation is read by the tensor core (async proxy)
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                asm volatile("tcgen05.fence::before_thread_sync;");
-                __syncwarp();
-                if (lane == 0)
-                    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];"
-                                 ::"r"(smem_addr(h_ready)) : "memory");
             }
         }
     }
@@ -842,7 +885,7 @@ __global__ void __launch_bounds__(FI_THREADS, 1)
     }
     if (warp == 1) {
         asm volatile("tcgen05.fence::after_thread_sync;");
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(256));
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
     }
 }
 
