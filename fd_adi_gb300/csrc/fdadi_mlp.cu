@@ -321,6 +321,27 @@ __device__ __forceinline__ bool ws_wait(uint64_t *mbar, uint32_t parity, volatil
     return true;
 }
 
+// ws_wait for barriers that complete slowly (a whole layer's MMAs or
+// epilogue): backs off with __nanosleep between polls so that waiting warps
+// leave the issue slots to the warps doing the work.
+__device__ __forceinline__ bool ws_wait_slow(uint64_t *mbar, uint32_t parity, volatile int *abort) {
+    const long long t0 = clock64();
+    uint32_t done = 0;
+    while (true) {
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+            "selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done) : "r"(smem_addr(mbar)), "r"(parity) : "memory");
+        if (done) return true;
+        if (*abort) return false;
+        if (clock64() - t0 > GM_WAIT_CYCLES) {
+            *abort = 1;
+            return false;
+        }
+        __nanosleep(64);
+    }
+}
+
 __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *map, int x, int y,
                                             int z, uint64_t *mbar) {
     asm volatile(
@@ -778,7 +799,7 @@ __global__ void __launch_bounds__(FI_THREADS, 1)
                         // this slot's previous epilogue has read its accumulator
                         // and written the activation this layer reads
                         const uint32_t Lz = (uint32_t)(j * FI_LAYERS + l);
-                        if (Lz > 0 && !ws_wait(&h_ready[z], (Lz - 1) & 1, abort)) { ok = false; break; }
+                        if (Lz > 0 && !ws_wait_slow(&h_ready[z], (Lz - 1) & 1, abort)) { ok = false; break; }
                         if (l == 0 && !ws_wait(&x_full[z], (uint32_t)j & 1, abort)) { ok = false; break; }
                         asm volatile("tcgen05.fence::after_thread_sync;");
                         const uint32_t idesc = umma_idesc(GM_BM, LN[l]);
@@ -831,41 +852,60 @@ __global__ void __launch_bounds__(FI_THREADS, 1)
                     const int m = mt * GM_BM + row;
                     const uint32_t Lz = (uint32_t)(j * FI_LAYERS + l);
                     int w = 1;
-                    if (lane == 0) w = ws_wait(&acc_full[z], Lz & 1, abort) ? 1 : 0;
+                    if (lane == 0) w = ws_wait_slow(&acc_full[z], Lz & 1, abort) ? 1 : 0;
                     if (!__shfl_sync(0xffffffffu, w, 0)) { ok = false; break; }
                     asm volatile("tcgen05.fence::after_thread_sync;");
                     const float *bias = f.bias[l] + p * f.bstride[l];
                     const uint32_t shz = sbase + FI_H + z * FI_H_BYTES;
                     const int cb = l < FI_LAYERS - 1 ? part * 64 : 0;
                     const int ce = l < FI_LAYERS - 1 ? cb + 64 : (part == 0 ? 8 : 0);
-                    for (int c0 = cb; c0 < ce; c0 += 8) {
-                        uint32_t r[8];
-                        const uint32_t taddr =
-                            tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(z * 256 + c0);
-                        asm volatile(
-                            "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
-                            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
-                              "=r"(r[6]), "=r"(r[7])
-                            : "r"(taddr));
-                        const float4 b0 = *reinterpret_cast<const float4 *>(bias + c0);
-                        const float4 b1 = *reinterpret_cast<const float4 *>(bias + c0 + 4);
-                        asm volatile("tcgen05.wait::ld.sync.aligned;");
-                        const float bb[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
-                        float x[8];
-#pragma unroll
-                        for (int e = 0; e < 8; ++e) x[e] = __uint_as_float(r[e]) + bb[e];
-                        if (l == FI_LAYERS - 1) {
+                    if (l == FI_LAYERS - 1) {
+                        if (ce > cb) {
+                            uint32_t r[8];
+                            const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(z * 256);
+                            asm volatile(
+                                "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+                                  "=r"(r[6]), "=r"(r[7])
+                                : "r"(taddr));
+                            asm volatile("tcgen05.wait::ld.sync.aligned;");
                             *reinterpret_cast<float2 *>(f.out + ((int64_t)p * f.M + m) * 2) =
-                                make_float2(x[0], x[1]);
-                        } else {
-                            __align__(16) __nv_bfloat162 h2[4];
+                                make_float2(__uint_as_float(r[0]) + bias[0], __uint_as_float(r[1]) + bias[1]);
+                        }
+                    } else {
+                        // 32 columns per tensor-memory load, one wait
+                        for (int c32 = cb; c32 < ce; c32 += 32) {
+                            uint32_t r[32];
+                            const uint32_t taddr =
+                                tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(z * 256 + c32);
+                            asm volatile(
+                                "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, "
+                                "%8, %9, %10, %11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, "
+                                "%23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+                                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+                                  "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]),
+                                  "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+                                  "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+                                  "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]),
+                                  "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+                                : "r"(taddr));
+                            asm volatile("tcgen05.wait::ld.sync.aligned;");
 #pragma unroll
-                            for (int e = 0; e < 4; ++e)
-                                h2[e] = __floats2bfloat162_rn(silu_fast(x[2 * e]), silu_fast(x[2 * e + 1]));
-                            const uint4 hv = *reinterpret_cast<const uint4 *>(h2);
-                            asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};"
-                                         ::"r"(shz + (c0 / 8) * GM_BM * 16 + row * 16), "r"(hv.x),
-                                           "r"(hv.y), "r"(hv.z), "r"(hv.w) : "memory");
+                            for (int g8 = 0; g8 < 32; g8 += 8) {
+                                const float4 b0 = *reinterpret_cast<const float4 *>(bias + c32 + g8);
+                                const float4 b1 = *reinterpret_cast<const float4 *>(bias + c32 + g8 + 4);
+                                const float bb[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+                                __align__(16) __nv_bfloat162 h2[4];
+#pragma unroll
+                                for (int e = 0; e < 4; ++e)
+                                    h2[e] = __floats2bfloat162_rn(
+                                        silu_fast(__uint_as_float(r[g8 + 2 * e]) + bb[2 * e]),
+                                        silu_fast(__uint_as_float(r[g8 + 2 * e + 1]) + bb[2 * e + 1]));
+                                const uint4 hv = *reinterpret_cast<const uint4 *>(h2);
+                                asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};"
+                                             ::"r"(shz + ((c32 + g8) / 8) * GM_BM * 16 + row * 16),
+                                               "r"(hv.x), "r"(hv.y), "r"(hv.z), "r"(hv.w) : "memory");
+                            }
                         }
                     }
                     // the activation is read by the tensor core (async proxy)
