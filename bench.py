@@ -163,7 +163,7 @@ class Clocks(object):
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
-        sm, mx, reasons = [], [], set()
+        sm, mx, pw, reasons = [], [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
             f = [x.strip() for x in ln.split(",")]
@@ -174,11 +174,17 @@ class Clocks(object):
                 mx.append(float(f[2]))
             except ValueError:
                 continue
+            try:
+                pw.append(float(f[3]))
+            except ValueError:
+                pass
             for nm, val in zip(names, f[5:9]):
                 if val.lower().startswith("active"):
                     reasons.add(nm)
         return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_min_mhz": float(min(sm)) if sm else None,
                 "sm_max_mhz": float(max(mx)) if mx else None,
+                "power_w": float(np.median(pw)) if pw else None,
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
@@ -665,7 +671,11 @@ def main():
     clk = clocks.stop()
     step_e2e()
     torch.cuda.synchronize()
+    clocks_e2e = Clocks(local)
+    clocks_e2e.start()
+    time.sleep(0.3)
     ms_e2e = timed(step_e2e, max(1, args.steps))
+    clk_e2e = clocks_e2e.stop()
 
     n_total = len(w_all["K"])
     value = n_total / (ms * 1e-3)
@@ -690,7 +700,8 @@ def main():
                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                "dtype": "f64", "data": "synthetic", "config": config_block(args, w),
                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-                       "d2h_bytes_per_step": int(d2h), "ms_per_step": ms_e2e},
+                       "d2h_bytes_per_step": int(d2h), "ms_per_step": ms_e2e,
+                       "clocks": clk_e2e},
                "gpu_launches": int(launches),
                "grid_point_steps_per_s": pts_steps * world / (ms * 1e-3),
                "roofline": {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": hbm_peak,
