@@ -1283,6 +1283,7 @@ int fdadi_mlp_gemm(const fdadi_gemm_t *a, void *stream) {
                               a->strideAux % 4 == 0),
                   "GEMM aux must be 16-byte aligned with ldaux, strideAux multiples of 4");
     FDADI_REQUIRE(a->problems >= 1, "GEMM needs at least one problem");
+    FDADI_REQUIRE(a->variant == 0 || a->variant == 1, "unknown GEMM variant %d", a->variant);
     static bool attr[64] = {false};
     int dev = 0;
     FDADI_CUDA(cudaGetDevice(&dev));
@@ -1296,7 +1297,6 @@ int fdadi_mlp_gemm(const fdadi_gemm_t *a, void *stream) {
                a->bias, a->strideBias, a->aux, a->ldaux, a->strideAux, a->out_f32, a->ldo,
                a->strideO, (bf16 *)a->out_bf16, a->ldh, a->strideH, a->M, a->N, a->K, a->act,
                a->status};
-    FDADI_REQUIRE(a->variant == 0 || a->variant == 1, "unknown GEMM variant %d", a->variant);
     if (a->variant == 0) return launch_ws(a, g, as_stream(stream));
     dim3 grid(a->M / 128, a->problems);
     umma_gemm_kernel<<<grid, GM_THREADS, GM_SMEM, as_stream(stream)>>>(g);

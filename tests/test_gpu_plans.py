@@ -269,3 +269,28 @@ def test_craig_sneyd_uneven_batch_vs_oracle(uneven, scheme, theta):
     b = HestonBatch(opts, meshes, **dict(kw, scheme=scheme, theta=theta),
                     plan=make_plan(SPOT_PLANS[0], VAR_PLANS[2], 2))
     _check(b.solve(V0), opts, meshes, want)
+
+
+@pytest.mark.parametrize("plan", [((0, 1, 128), (0, 4)), ((1, 8, 128), (3, 16)),
+                                  ((0, 8, 32), (1, 2)), ((1, 32, 4), (2, 1))])
+@pytest.mark.parametrize("scheme", ["hv", "douglas", "mcs"])
+def test_minimum_and_ragged_grids_vs_oracle(cuda, plan, scheme):
+    """The smallest grids the reference accepts (4 points per line,
+    BandedOperator.pyx:43) mixed with ragged ones (sizes that fill no tile,
+    chunk or segment evenly) in one batch, against the oracle."""
+    from fd_adi_gb300.batch import HestonBatch, make_plan
+    sizes = [(4, 4), (5, 7), (17, 33), (4, 40), (33, 4), (6, 5), (64, 37)]
+    meshes = [(800.0 * np.linspace(0, 1, a) ** 1.5, 5.0 * np.linspace(0, 1, b) ** 2) for a, b in sizes]
+    params = [(0.03 + 0.005 * k, 1.5, 0.05, 0.4, -0.5 + 0.05 * k) for k in range(len(sizes))]
+    V0 = [np.maximum(m[0][:, None] - 100.0, 0) * np.ones((1, m[1].size)) for m in meshes]
+    theta = {"hv": HV_THETA, "douglas": 0.5, "mcs": 1.0 / 3}[scheme]
+    dt, n = 0.01, 10
+    b = HestonBatch(params, meshes, scheme=scheme, n_steps=n, dt=dt, theta=theta,
+                    implicit_steps=2, implicit_dt_factor=0.5, plan=make_plan(*plan))
+    out = b.solve(V0)
+    for k, m in enumerate(meshes):
+        ref = O.heston_solve(m[0], m[1], *params[k], V0[k],
+                             [("implicit", 2, dt / 2, 1.0), (scheme, n, dt, theta)])
+        assert np.isfinite(out[k]).all(), sizes[k]
+        assert _rel(out[k], ref) < 1e-11, (sizes[k], _rel(out[k], ref))
+    assert not b.status(b.pack(out)).any()
