@@ -321,6 +321,16 @@ __device__ __forceinline__ bool ws_wait(uint64_t *mbar, uint32_t parity, volatil
     return true;
 }
 
+// Non-blocking test of an mbarrier phase.
+__device__ __forceinline__ bool mbar_test(uint64_t *mbar, uint32_t parity) {
+    uint32_t done = 0;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        "selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done) : "r"(smem_addr(mbar)), "r"(parity) : "memory");
+    return done != 0;
+}
+
 // ws_wait for barriers that complete slowly (a whole layer's MMAs or
 // epilogue): backs off with __nanosleep between polls so that waiting warps
 // leave the issue slots to the warps doing the work.
@@ -652,10 +662,12 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
 // the next layer's MMA reads as its A operand. Only the weights stream in (TMA,
 // 32-wide K chunks through a ring, L2-resident across units) and only the two
 // outputs per query and member go out. The layers of one unit form a strict
-// chain, so each CTA keeps two units in flight (slots 0 and 1, each with its
-// own query tile, activation tile and 256-column accumulator) and interleaves
-// them layer by layer: the epilogue of one slot runs while the MMAs of the
-// other do. Roles:
+// chain, so each CTA keeps two units in flight: slots 0 and 1 hold two
+// adjacent 128-query tiles of one member, each with its own query tile,
+// activation tile and 256-column accumulator. Every weight chunk is loaded
+// once and multiplied into both accumulators, which halves the weight stream
+// per query. Slot 0 may run up to a ring's worth of chunks ahead of slot 1, so
+// one slot's epilogue partly overlaps the other's MMAs. Roles:
 //   warp 0 (one lane): TMA producer for the query tiles and the weight chunks,
 //     in the order the MMAs consume them, running ahead across layers;
 //   warp 1: tensor-memory owner; one lane issues each (layer, slot)'s MMAs once
@@ -702,11 +714,11 @@ __global__ void __launch_bounds__(FI_THREADS, 1)
     volatile int *abort = reinterpret_cast<volatile int *>(tslot + 1);
     const uint32_t sbase = smem_addr(smem);
     const uint32_t sring = sbase + FI_RING;
-    const int units = f.m_tiles * f.members;
-    // unit k of this CTA is blockIdx.x + k * gridDim.x, in slot k % 2; pair j
-    // holds units 2j and 2j + 1
-    const int nmine = units > (int)blockIdx.x ? (units - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
-    const int npairs = (nmine + 1) / 2;
+    // a pair is two adjacent 128-query tiles of one member (the second absent
+    // when the member has an odd number of tiles); this CTA takes pairs
+    // blockIdx.x, blockIdx.x + gridDim.x, ...
+    const int halft = (f.m_tiles + 1) / 2;
+    const int npairs_all = f.members * halft;
     // layer l: K, N of the MMA (the last layer uses its first 16 outputs)
     const int LK[FI_LAYERS] = {16, 256, 256, 256, 256};
     const int LN[FI_LAYERS] = {256, 256, 256, 256, 16};
@@ -740,35 +752,33 @@ __global__ void __launch_bounds__(FI_THREADS, 1)
     if (warp == 0) {
         if (lane == 0) {
             const CUtensorMap *maps[FI_LAYERS] = {&tw0, &tw1, &tw2, &tw3, &tw4};
-            uint32_t it = 0;
+            uint32_t it = 0, xc[2] = {0u, 0u};
             bool ok = true;
-            for (int j = 0; j < npairs && ok; ++j) {
-                const int nz = min(2, nmine - 2 * j);
+            for (int pi = blockIdx.x; pi < npairs_all && ok; pi += gridDim.x) {
+                const int p = pi / halft, t = pi % halft;
+                const int nz = (2 * t + 1 < f.m_tiles) ? 2 : 1;
                 for (int z = 0; z < nz; ++z) {
-                    const int u = blockIdx.x + (2 * j + z) * gridDim.x;
-                    const int mt = u % f.m_tiles;
-                    if (j > 0 && !ws_wait(&x_empty[z], (uint32_t)(j - 1) & 1, abort)) { ok = false; break; }
+                    if (xc[z] > 0 && !ws_wait(&x_empty[z], (xc[z] - 1) & 1, abort)) { ok = false; break; }
                     const uint32_t sx = sbase + z * FI_X_BYTES;
                     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
                                  ::"r"(smem_addr(&x_full[z])), "r"(FI_X_BYTES) : "memory");
-                    tma_load_3d(sx, &tmX, 0, mt * GM_BM, 0, &x_full[z]);
-                    tma_load_3d(sx + GM_BM * 16, &tmX, 8, mt * GM_BM, 0, &x_full[z]);
+                    tma_load_3d(sx, &tmX, 0, (2 * t + z) * GM_BM, 0, &x_full[z]);
+                    tma_load_3d(sx + GM_BM * 16, &tmX, 8, (2 * t + z) * GM_BM, 0, &x_full[z]);
+                    ++xc[z];
                 }
+                // each weight chunk once per pair: both tiles multiply it
                 for (int l = 0; l < FI_LAYERS && ok; ++l) {
-                    for (int z = 0; z < nz && ok; ++z) {
-                        const int p = (int)((blockIdx.x + (2 * j + z) * gridDim.x) / f.m_tiles);
-                        for (int k0 = 0; k0 < LK[l]; k0 += FI_BK, ++it) {
-                            const int s = it % FI_STAGES;
-                            const uint32_t n = it / FI_STAGES;
-                            if (n > 0 && !ws_wait(&empty[s], (n - 1) & 1, abort)) { ok = false; break; }
-                            const int kc = min(FI_BK, LK[l] - k0) >> 3;
-                            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
-                                         ::"r"(smem_addr(&full[s])), "r"((uint32_t)(kc * LN[l] * 16))
-                                         : "memory");
-                            const uint32_t b0 = sring + s * FI_STAGE_BYTES;
-                            for (int c = 0; c < kc; ++c)
-                                tma_load_3d(b0 + c * LN[l] * 16, maps[l], k0 + 8 * c, 0, p, &full[s]);
-                        }
+                    for (int k0 = 0; k0 < LK[l]; k0 += FI_BK, ++it) {
+                        const int s = it % FI_STAGES;
+                        const uint32_t n = it / FI_STAGES;
+                        if (n > 0 && !ws_wait(&empty[s], (n - 1) & 1, abort)) { ok = false; break; }
+                        const int kc = min(FI_BK, LK[l] - k0) >> 3;
+                        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                                     ::"r"(smem_addr(&full[s])), "r"((uint32_t)(kc * LN[l] * 16))
+                                     : "memory");
+                        const uint32_t b0 = sring + s * FI_STAGE_BYTES;
+                        for (int c = 0; c < kc; ++c)
+                            tma_load_3d(b0 + c * LN[l] * 16, maps[l], k0 + 8 * c, 0, p, &full[s]);
                     }
                 }
             }
@@ -780,58 +790,108 @@ __global__ void __launch_bounds__(FI_THREADS, 1)
                 if (*abort) mbar_wait(&full[s], n & 1);
                 else ws_wait(&empty[s], n & 1, abort);
             }
-            if (*abort) {
-                // the last query tile of each slot
-                for (int z = 0; z < 2; ++z) {
-                    const int cnt = (nmine - z + 1) / 2;   // tiles loaded into slot z (at most)
-                    if (cnt > 0) mbar_wait(&x_full[z], (uint32_t)(cnt - 1) & 1);
-                }
-            }
+            if (*abort)
+                for (int z = 0; z < 2; ++z)
+                    if (xc[z] > 0) mbar_wait(&x_full[z], (xc[z] - 1) & 1);
         }
     } else if (warp == 1) {
         if (lane == 0) {
-            uint32_t it = 0;
+            uint32_t it = 0, xc[2] = {0u, 0u}, Lz[2] = {0u, 0u};
             bool ok = true;
-            for (int j = 0; j < npairs && ok; ++j) {
-                const int nz = min(2, nmine - 2 * j);
-                for (int l = 0; l < FI_LAYERS && ok; ++l) {
-                    for (int z = 0; z < nz && ok; ++z) {
-                        // this slot's previous epilogue has read its accumulator
-                        // and written the activation this layer reads
-                        const uint32_t Lz = (uint32_t)(j * FI_LAYERS + l);
-                        if (Lz > 0 && !ws_wait_slow(&h_ready[z], (Lz - 1) & 1, abort)) { ok = false; break; }
-                        if (l == 0 && !ws_wait(&x_full[z], (uint32_t)j & 1, abort)) { ok = false; break; }
-                        asm volatile("tcgen05.fence::after_thread_sync;");
-                        const uint32_t idesc = umma_idesc(GM_BM, LN[l]);
-                        const uint32_t abase = l == 0 ? sbase + z * FI_X_BYTES
-                                                      : sbase + FI_H + z * FI_H_BYTES;
-                        const uint32_t d = tmem + (uint32_t)(z * 256);
-                        bool first = true;
-                        for (int k0 = 0; k0 < LK[l]; k0 += FI_BK, ++it) {
-                            const int s = it % FI_STAGES;
-                            const uint32_t n = it / FI_STAGES;
-                            if (!ws_wait(&full[s], n & 1, abort)) { ok = false; break; }
-                            asm volatile("tcgen05.fence::after_thread_sync;");
-                            const int kw = min(FI_BK, LK[l] - k0);
-                            const uint32_t b0 = sring + s * FI_STAGE_BYTES;
-                            for (int q = 0; q < (kw >> 4); ++q) {
-                                const uint64_t ad = umma_desc(abase + (k0 / 8 + 2 * q) * GM_BM * 16,
-                                                              GM_BM * 16, 128);
-                                const uint64_t bd = umma_desc(b0 + q * 2 * LN[l] * 16, LN[l] * 16, 128);
-                                const uint32_t accum = first ? 0u : 1u;
-                                first = false;
-                                asm volatile(
-                                    "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-                                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
-                                    ::"r"(d), "l"(ad), "l"(bd), "r"(idesc), "r"(accum));
-                            }
-                            tcgen05_commit(&empty[s]);
-                        }
-                        if (!ok) break;
-                        if (l == 0) tcgen05_commit(&x_empty[z]);
-                        tcgen05_commit(&acc_full[z]);
+            // slot z of the current pair may take a layer once its previous
+            // epilogue has released the accumulator (and, for layer 0, its
+            // query tile has landed)
+            auto slot_ready = [&](int z, int l, bool block) -> int {
+                if (Lz[z] > 0) {
+                    if (block) {
+                        if (!ws_wait_slow(&h_ready[z], (Lz[z] - 1) & 1, abort)) return -1;
+                    } else if (!mbar_test(&h_ready[z], (Lz[z] - 1) & 1)) {
+                        return 0;
                     }
                 }
+                if (l == 0) {
+                    if (block) {
+                        if (!ws_wait(&x_full[z], xc[z] & 1, abort)) return -1;
+                    } else if (!mbar_test(&x_full[z], xc[z] & 1)) {
+                        return 0;
+                    }
+                }
+                return 1;
+            };
+            auto issue = [&](int z, int l, uint32_t stage, int q0, bool first) {
+                const uint32_t idesc = umma_idesc(GM_BM, LN[l]);
+                const uint32_t abase = l == 0 ? sbase + z * FI_X_BYTES : sbase + FI_H + z * FI_H_BYTES;
+                const uint32_t d = tmem + (uint32_t)(z * 256);
+                const uint32_t b0 = sring + stage * FI_STAGE_BYTES;
+                const int kw = min(FI_BK, LK[l] - q0);
+                for (int q = 0; q < (kw >> 4); ++q) {
+                    const uint64_t ad = umma_desc(abase + (q0 / 8 + 2 * q) * GM_BM * 16, GM_BM * 16, 128);
+                    const uint64_t bd = umma_desc(b0 + q * 2 * LN[l] * 16, LN[l] * 16, 128);
+                    const uint32_t accum = (first && q == 0) ? 0u : 1u;
+                    asm volatile(
+                        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+                        ::"r"(d), "l"(ad), "l"(bd), "r"(idesc), "r"(accum));
+                }
+            };
+            for (int pi = blockIdx.x; pi < npairs_all && ok; pi += gridDim.x) {
+                const int t = pi % halft;
+                const int nz = (2 * t + 1 < f.m_tiles) ? 2 : 1;
+                for (int l = 0; l < FI_LAYERS && ok; ++l) {
+                    if (slot_ready(0, l, true) < 0) { ok = false; break; }
+                    asm volatile("tcgen05.fence::after_thread_sync;");
+                    const int nch = (LK[l] + FI_BK - 1) / FI_BK;
+                    const uint32_t it0 = it;
+                    bool ready1 = nz < 2;   // nothing to issue for an absent tile
+                    int pend = 0;           // next chunk slot 1 has to multiply
+                    auto flush1 = [&](int upto) {
+                        for (; pend < upto; ++pend) {
+                            const uint32_t st = (it0 + pend) % FI_STAGES;
+                            issue(1, l, st, pend * FI_BK, pend == 0);
+                            tcgen05_commit(&empty[st]);
+                        }
+                    };
+                    for (int kk = 0; kk < nch; ++kk, ++it) {
+                        if (nz == 2 && !ready1 && kk - pend >= FI_STAGES) {
+                            // every stage holds a chunk slot 1 still needs
+                            const int r = slot_ready(1, l, true);
+                            if (r < 0) { ok = false; break; }
+                            ready1 = true;
+                            asm volatile("tcgen05.fence::after_thread_sync;");
+                            flush1(kk);
+                        }
+                        const int s = it % FI_STAGES;
+                        const uint32_t n = it / FI_STAGES;
+                        if (!ws_wait(&full[s], n & 1, abort)) { ok = false; break; }
+                        asm volatile("tcgen05.fence::after_thread_sync;");
+                        issue(0, l, (uint32_t)s, kk * FI_BK, kk == 0);
+                        if (nz == 2) {
+                            if (!ready1 && slot_ready(1, l, false) == 1) {
+                                ready1 = true;
+                                asm volatile("tcgen05.fence::after_thread_sync;");
+                            }
+                            if (ready1) flush1(kk + 1);
+                        } else {
+                            tcgen05_commit(&empty[s]);
+                        }
+                    }
+                    if (!ok) break;
+                    if (l == 0) tcgen05_commit(&x_empty[0]);
+                    tcgen05_commit(&acc_full[0]);
+                    ++Lz[0];
+                    if (nz == 2) {
+                        if (!ready1) {
+                            if (slot_ready(1, l, true) < 0) { ok = false; break; }
+                            asm volatile("tcgen05.fence::after_thread_sync;");
+                        }
+                        flush1(nch);
+                        if (l == 0) tcgen05_commit(&x_empty[1]);
+                        tcgen05_commit(&acc_full[1]);
+                        ++Lz[1];
+                    }
+                }
+                ++xc[0];
+                if (nz == 2) ++xc[1];
             }
             if (*abort) {
                 tcgen05_commit(drain);
@@ -842,17 +902,16 @@ __global__ void __launch_bounds__(FI_THREADS, 1)
         // epilogue: warp w -> TMEM lanes 32 (w % 4) ..., column quarter (w - 2) / 4
         const int q = warp & 3, part = (warp - 2) >> 2;
         const int row = q * 32 + lane;
+        uint32_t Lz[2] = {0u, 0u};
         bool ok = true;
-        for (int j = 0; j < npairs && ok; ++j) {
-            const int nz = min(2, nmine - 2 * j);
+        for (int pi = blockIdx.x; pi < npairs_all && ok; pi += gridDim.x) {
+            const int p = pi / halft, t = pi % halft;
+            const int nz = (2 * t + 1 < f.m_tiles) ? 2 : 1;
             for (int l = 0; l < FI_LAYERS && ok; ++l) {
                 for (int z = 0; z < nz; ++z) {
-                    const int u = blockIdx.x + (2 * j + z) * gridDim.x;
-                    const int mt = u % f.m_tiles, p = u / f.m_tiles;
-                    const int m = mt * GM_BM + row;
-                    const uint32_t Lz = (uint32_t)(j * FI_LAYERS + l);
+                    const int m = (2 * t + z) * GM_BM + row;
                     int w = 1;
-                    if (lane == 0) w = ws_wait_slow(&acc_full[z], Lz & 1, abort) ? 1 : 0;
+                    if (lane == 0) w = ws_wait_slow(&acc_full[z], Lz[z] & 1, abort) ? 1 : 0;
                     if (!__shfl_sync(0xffffffffu, w, 0)) { ok = false; break; }
                     asm volatile("tcgen05.fence::after_thread_sync;");
                     const float *bias = f.bias[l] + p * f.bstride[l];
@@ -915,6 +974,7 @@ __global__ void __launch_bounds__(FI_THREADS, 1)
                     if (lane == 0)
                         asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];"
                                      ::"r"(smem_addr(&h_ready[z])) : "memory");
+                    ++Lz[z];
                 }
             }
         }
@@ -1252,8 +1312,8 @@ int fdadi_mlp_infer(const fdadi_mlp_net_t *net, const void *X, int32_t M, float 
     f.m_tiles = M / GM_BM;
     f.members = net->members;
     f.status = status;
-    const int units = f.m_tiles * f.members;
-    const unsigned grid = (unsigned)std::min(units, sm_count());
+    const int pairs = f.members * ((f.m_tiles + 1) / 2);
+    const unsigned grid = (unsigned)std::min(pairs, sm_count());
     mlp_infer_kernel<<<grid, FI_THREADS, FI_SMEM, as_stream(stream)>>>(mX, mW[0], mW[1], mW[2],
                                                                       mW[3], mW[4], f);
     FDADI_CHECK_LAUNCH();

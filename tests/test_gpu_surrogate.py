@@ -121,12 +121,15 @@ def test_surrogate_learns_adi_prices_and_gates(dev):
     assert t_sur * 100 < t_adi
 
 
-def test_fused_inference_matches_layered_forward(dev):
+@pytest.mark.parametrize("tiles", [200, 33, 1])
+def test_fused_inference_matches_layered_forward(dev, tiles):
     """The one-kernel inference against the layer-by-layer tensor-core forward
     on the same bf16 weights: both round activations to bf16 at the same
-    points, so they agree to accumulation order (1e-3 of the output scale)."""
+    points, so they agree to accumulation order (1e-3 of the output scale).
+    200 tiles: more tile pairs than SMs, so every CTA loops; 33 and 1: an odd
+    tile count leaves each member's last pair with one tile."""
     from fd_adi_gb300.surrogate import MLPEnsemble
-    M = 128 * 200              # more tiles than SMs: every CTA loops over units
+    M = 128 * tiles
     net = MLPEnsemble(members=4, seed=5, device=dev)
     g = torch.Generator(device="cpu").manual_seed(2)
     for li in range(len(net.b)):
