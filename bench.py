@@ -617,7 +617,13 @@ def main():
     h_vars = batch.vars.cpu().pin_memory()
     h_params = batch.params.cpu().pin_memory()
     h_dt = batch.dt.cpu().pin_memory()
-    h_V0 = V0_dev.cpu().pin_memory()
+    # the initial grids are the calls' payoffs, built on the device from the
+    # strikes (checked once against the host-built grids)
+    K_dev = torch.tensor(w["K"], dtype=torch.float64, device="cuda")
+    h_K = K_dev.cpu().pin_memory()
+    batch._prepare()
+    if not torch.equal(batch.payoff(K_dev, V), V0_dev):
+        raise RuntimeError("device payoff differs from the host-built initial grids")
     flat_idx = batch.flat_index([(w["S0"], v0) for v0 in w["v0"]])
     prices = torch.empty(batch.n, dtype=torch.float64, device="cuda")
     h_prices = torch.empty(batch.n, dtype=torch.float64).pin_memory()
@@ -626,7 +632,7 @@ def main():
     def step_device():
         with torch.cuda.stream(stream):
             batch._prepare()
-            V.copy_(V0_dev, non_blocking=True)
+            batch.payoff(K_dev, V)
             batch.run(V)
             batch.gather(V, flat_idx, prices)
 
@@ -636,8 +642,9 @@ def main():
             batch.vars.copy_(h_vars, non_blocking=True)
             batch.params.copy_(h_params, non_blocking=True)
             batch.dt.copy_(h_dt, non_blocking=True)
-            V.copy_(h_V0, non_blocking=True)
+            K_dev.copy_(h_K, non_blocking=True)
             batch._prepare()
+            batch.payoff(K_dev, V)
             batch.run(V)
             batch.gather(V, flat_idx, prices)
             h_prices.copy_(prices, non_blocking=True)
@@ -680,9 +687,10 @@ def main():
     n_total = len(w_all["K"])
     value = n_total / (ms * 1e-3)
     e2e_value = n_total / (ms_e2e * 1e-3)
-    h2d = sum(t.numel() * t.element_size() for t in (h_spots, h_vars, h_params, h_dt, h_V0))
+    h2d = sum(t.numel() * t.element_size() for t in (h_spots, h_vars, h_params, h_dt, h_K))
     d2h = h_prices.numel() * 8
-    launches = args.steps * (batch.launches_per_run + 3 + 1)
+    # per step: the run, 4 prepare kernels, the payoff and the price gather
+    launches = args.steps * (batch.launches_per_run + 4 + 2)
 
     out = None
     if rank == 0:

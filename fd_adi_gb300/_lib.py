@@ -138,6 +138,9 @@ SIGNATURES = {
                                            ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
                                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                            ctypes.c_void_p]),
+    "fdadi_heston_payoff": (ctypes.c_int, [ctypes.POINTER(HestonBatch), ctypes.c_void_p,
+                                           ctypes.c_int64, ctypes.c_void_p, ctypes.c_int32,
+                                           ctypes.c_void_p, ctypes.c_void_p]),
     "fdadi_heston_status": (ctypes.c_int, [ctypes.POINTER(HestonBatch), ctypes.c_void_p,
                                            ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
                                            ctypes.c_void_p]),

@@ -239,6 +239,18 @@ class HestonBatch(object):
             torch.cuda.current_stream(self.device).wait_stream(self.stream)
         return V
 
+    def payoff(self, strikes, V=None, put=False):
+        """Initial state built on the device: max(S - K, 0) (or the put's
+        max(K - S, 0)) on every option's mesh. strikes: device float64 [n]."""
+        if V is None:
+            V = torch.empty(self.total_points, dtype=torch.float64, device=self.device)
+        cur = torch.cuda.current_stream(self.device)
+        _lib.call("fdadi_heston_payoff", ctypes.byref(self.struct),
+                  ctypes.c_void_p(self.workspace.data_ptr()), self.workspace_bytes,
+                  ctypes.c_void_p(strikes.data_ptr()), 1 if put else 0,
+                  ctypes.c_void_p(V.data_ptr()), ctypes.c_void_p(cur.cuda_stream))
+        return V
+
     def greeks(self, V, flat_idx):
         """(price, delta, gamma) device tensors: each option's value at its
         arena index and the centred non-uniform S-derivatives there."""

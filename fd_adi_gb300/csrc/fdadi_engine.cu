@@ -89,6 +89,7 @@ struct Arena {
     double *w0i, *RSi, *LSi, *LVvi, *foldVi, *LVzi;
     // HV corrector: (1/2 - theta) * F0 [3P] and w0 / 2 [3 SS]
     double *F0h, *w0h;
+    double *sw;                // [6 SS] spot stencil weights for the builders
     // stage buffers
     double *FV, *W, *T, *Y2;
     const double *theta;       // [n_opt]
@@ -119,12 +120,38 @@ __device__ __forceinline__ void centre(const double *x, int i, int derivative, d
     }
 }
 
+
+// The spot-index parts of a spot operator row, computed once per (option, i)
+// so that the per-point builders do no division: w[0..5] = centred first and second
+// derivative weights (sub, mid, sup) at an interior row; on the last row
+// w[0..2] = the "first derivative = 1" row's mid2, sub2 and R2. Stored at
+// w[k * SS + s_off + i].
+__device__ void spot_weights(const double *S, int n, int i, double *w, int64_t SS) {
+    if (i == 0) return;
+    if (i == n - 1) {
+        const double dm1 = SUB(S[n - 1], S[n - 2]);
+        const double xx = MUL(dm1, dm1);
+        w[0] = DIV(-2.0, xx);
+        w[SS] = DIV(2.0, xx);
+        w[2 * SS] = DIV(MUL(1.0, 2.0), dm1);
+        return;
+    }
+    double s1, m1, p1, s2, m2, p2;
+    centre(S, i, 1, s1, m1, p1);
+    centre(S, i, 2, s2, m2, p2);
+    w[0] = s1; w[SS] = m1; w[2 * SS] = p1;
+    w[3 * SS] = s2; w[4 * SS] = m2; w[5 * SS] = p2;
+}
+
 // Combined spot operator A0 = r S D_S + 1/2 v S^2 D_SS - r/2 at row i of the
 // spot line through variance v_j: boundaries heston.py:337-342 (Dirichlet
 // U = 0 at S = 0, dU/dS = 1 at S_max) or the up-and-out Dirichlet row at S_max
 // (heston.py:361-370); combination FiniteDifferenceEngine.pyx:563-592.
-__device__ Row3 spot_row(const double *S, int n, int i, double vj, double r, float half_r,
-                         bool barrier) {
+// The stencil weights come precomputed per spot index (spot_weights); every
+// per-point operation is the reference's, in its order, so the rows are
+// bit-identical to building them from the mesh directly.
+__device__ Row3 spot_row_w(const double *w, int64_t SS, const double *S, int n, int i, double vj,
+                           double r, float half_r, bool barrier) {
     Row3 o{0.0, 0.0, 0.0, 0.0, 0.0, false};
     if (i == 0 || (i == n - 1 && barrier)) {
         o.mid = 1.0;
@@ -135,19 +162,15 @@ __device__ Row3 spot_row(const double *S, int n, int i, double vj, double r, flo
     const double c0 = MUL(r, S[i]);
     const double c00 = MUL(MUL(0.5, vj), MUL(S[i], S[i]));
     if (i == n - 1) {
-        const double dm1 = SUB(S[n - 1], S[n - 2]);
-        const double xx = MUL(dm1, dm1);
-        const double mid2 = DIV(-2.0, xx), sub2 = DIV(2.0, xx);
-        const double R2 = DIV(MUL(1.0, 2.0), dm1);
+        const double mid2 = w[0], sub2 = w[SS], R2 = w[2 * SS];
         o.mid = ADD(ADD(MUL(0.0, c0), f), MUL(mid2, c00));
         o.sub = ADD(MUL(0.0, c0), MUL(sub2, c00));
         o.sup = 0.0;
         o.R = ADD(MUL(1.0, c0), MUL(R2, c00));
         return o;
     }
-    double s1, m1, p1, s2, m2, p2;
-    centre(S, i, 1, s1, m1, p1);
-    centre(S, i, 2, s2, m2, p2);
+    const double s1 = w[0], m1 = w[SS], p1 = w[2 * SS], s2 = w[3 * SS], m2 = w[4 * SS],
+                 p2 = w[5 * SS];
     o.sup = ADD(MUL(p1, c0), MUL(p2, c00));
     o.mid = ADD(ADD(MUL(m1, c0), f), MUL(m2, c00));
     o.sub = ADD(MUL(s1, c0), MUL(s2, c00));
@@ -261,6 +284,15 @@ __device__ void var_factors(const Arena &A, int o, const double *v, int n1, doub
     if (t.bad || !isfinite(*zinv) || !isfinite(f)) atomicOr(&A.ostat[o], FDADI_STATUS_PIVOT);
 }
 
+// One block per option: the spot-index weights of spot_row_w.
+__global__ void build_spot_weights_kernel(Arena A, BuildArgs a) {
+    const int o = blockIdx.x;
+    const int n0 = A.n0[o];
+    const int64_t so = A.s_off[o];
+    const double *S = a.spots + so;
+    for (int i = threadIdx.x; i < n0; i += blockDim.x) spot_weights(S, n0, i, A.sw + so + i, A.SS);
+}
+
 __global__ void build_options_kernel(Arena A, BuildArgs a) {
     const int o = blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= A.n_opt) return;
@@ -305,7 +337,8 @@ __global__ void build_points_kernel(Arena A, BuildArgs a) {
     const double dt = a.dt[o];
     const double dti = MUL(dt, a.dt_factor);
 
-    const Row3 s = spot_row(S, n0, i, v[j], r, half_r, barrier);
+    const double *swo = A.sw + A.s_off[o];
+    const Row3 s = spot_row_w(swo + i, A.SS, S, n0, i, v[j], r, half_r, barrier);
     double f0[3];
     if (s.dirichlet) {
         f0[0] = 0.0; f0[1] = 1.0; f0[2] = 0.0;
@@ -342,7 +375,7 @@ __global__ void build_points_kernel(Arena A, BuildArgs a) {
         A.w1[q] = sb * v[j]; A.w1[A.SV + q] = md * v[j]; A.w1[2 * A.SV + q] = sp * v[j];
         A.dirS[q] = 0.0;
         A.dirS[A.SV + q] = 0.0;
-        const Row3 top = spot_row(S, n0, n0 - 1, v[j], r, half_r, barrier);
+        const Row3 top = spot_row_w(swo + n0 - 1, A.SS, S, n0, n0 - 1, v[j], r, half_r, barrier);
         A.R0top[q] = top.dirichlet ? top.R : MUL(top.R, dt);
         if (a.smoothing) A.RSi[q] = top.dirichlet ? top.R : MUL(top.R, -dti);
         const Row3 w = var_row(v, n1, j, 1.0, r, half_r, kappa, th, sigma);
@@ -365,10 +398,11 @@ __global__ void build_spot_lines_kernel(Arena A, BuildArgs a) {
     const bool barrier = a.barrier && a.barrier[o];
     const double dt = a.dt[o];
     const double sm = MUL(a.theta, -dt), si = -MUL(dt, a.dt_factor);
+    const double *swo = A.sw + A.s_off[o];
     Thomas tm, ti;
     for (int i = 0; i < n0; ++i) {
         const int64_t p = A.p_off[o] + (int64_t)i * n1 + j;
-        const Row3 s = spot_row(S, n0, i, v[j], r, half_r, barrier);
+        const Row3 s = spot_row_w(swo + i, A.SS, S, n0, i, v[j], r, half_r, barrier);
         double sb = 0.0, md = 1.0, sp = 0.0;
         if (!s.dirichlet) { sb = MUL(s.sub, sm); md = ADD(MUL(s.mid, sm), 1.0); sp = MUL(s.sup, sm); }
         tm.row(A.LS, A.P, p, sb, md, sp, i == 0);
@@ -1161,6 +1195,19 @@ __global__ void __launch_bounds__(NSEG * 32) var_seg_kernel(Arena A, Span tasks,
     }
 }
 
+// Initial grid of a European call or put on every option's mesh (the
+// reference's grid initializer, heston.py:402): V = max(S_i - K, 0) (call) or
+// max(K - S_i, 0) (put) on every variance point; one block per tile.
+__global__ void payoff_kernel(Arena A, const double *spots, const double *strikes, int put,
+                              double *V) {
+    const int4 t = A.tiles[blockIdx.x];
+    const int o = t.x, n0 = A.n0[o], n1 = A.n1[o];
+    const int i = t.y + threadIdx.x / TJ, j = t.z + threadIdx.x % TJ;
+    if (i >= n0 || j >= n1) return;
+    const double S = spots[A.s_off[o] + i], K = strikes[o];
+    V[A.p_off[o] + (int64_t)i * n1 + j] = put ? fmax(K - S, 0.0) : fmax(S - K, 0.0);
+}
+
 // Per-option status: the build's pivot flags, plus FDADI_STATUS_NONFINITE if
 // any value of the option's state grid is NaN or infinite (one block per option).
 __global__ void status_kernel(Arena A, const double *V, int *out) {
@@ -1235,7 +1282,7 @@ struct Layout {
     int64_t o_F0, o_w0, o_w1, o_LS, o_R0top, o_F1v, o_F1x, o_F1z, o_LVv, o_foldV, o_LVz,
         o_dirS;
     int64_t o_w0i, o_RSi, o_LSi, o_LVvi, o_foldVi, o_LVzi;
-    int64_t o_FV, o_W, o_T, o_Y2, o_F0h, o_w0h;
+    int64_t o_FV, o_W, o_T, o_Y2, o_F0h, o_w0h, o_sw;
     int64_t bytes = 0;
     std::vector<int64_t> p_off, s_off, v_off, tile_off, task_off;
 };
@@ -1287,6 +1334,7 @@ static int make_layout(const fdadi_heston_batch_t *b, Layout &L) {
     L.o_vtasks = take(16 * L.n_vtasks); L.o_theta = take(D * N);
     L.o_ostat = take(4 * N);
     L.o_F0 = take(3 * D * L.P);
+    L.o_sw = take(6 * D * L.SS);
     L.o_w0 = take(3 * D * L.SS); L.o_w1 = take(3 * D * L.SV);
     L.o_LS = take(3 * D * L.P); L.o_R0top = take(D * L.SV); L.o_F1v = take(3 * D * L.SV);
     L.o_F1x = take(D * N); L.o_F1z = take(D * N); L.o_LVv = take(3 * D * L.SV);
@@ -1328,7 +1376,7 @@ static Arena arena_view(const Layout &L, char *ws) {
     A.w0i = ptr(L.o_w0i); A.RSi = ptr(L.o_RSi); A.LSi = ptr(L.o_LSi); A.LVvi = ptr(L.o_LVvi);
     A.foldVi = ptr(L.o_foldVi); A.LVzi = ptr(L.o_LVzi);
     A.FV = ptr(L.o_FV); A.W = ptr(L.o_W); A.T = ptr(L.o_T); A.Y2 = ptr(L.o_Y2);
-    A.F0h = ptr(L.o_F0h); A.w0h = ptr(L.o_w0h);
+    A.F0h = ptr(L.o_F0h); A.w0h = ptr(L.o_w0h); A.sw = ptr(L.o_sw);
     return A;
 }
 
@@ -1801,6 +1849,8 @@ int fdadi_heston_prepare(const fdadi_heston_batch_t *b, void *workspace, int64_t
     BuildArgs a{b->spots, b->vars, b->params, b->dt, b->barrier, b->theta, b->implicit_dt_factor,
                 L.smoothing ? 1 : 0, (b->flags & FDADI_HESTON_DROP_ZERO_MIXED) ? 1 : 0,
                 L.hv ? 1 : 0};
+    build_spot_weights_kernel<<<(unsigned)L.n_opt, 128, 0, st>>>(A, a);
+    FDADI_CHECK_LAUNCH();
     build_options_kernel<<<(unsigned)((L.n_opt + 127) / 128), 128, 0, st>>>(A, a);
     FDADI_CHECK_LAUNCH();
     build_points_kernel<<<(unsigned)L.n_tiles, EXPL_THREADS, 0, st>>>(A, a);
@@ -1877,6 +1927,21 @@ int fdadi_heston_stage(const fdadi_heston_batch_t *b, void *workspace, int64_t w
     rc = grids(b, L, g);
     if (rc) return rc;
     launch_stage(stage, g, A, V, as_stream(stream));
+    FDADI_CHECK_LAUNCH();
+    return FDADI_OK;
+}
+
+int fdadi_heston_payoff(const fdadi_heston_batch_t *b, void *workspace, int64_t ws_bytes,
+                        const double *strikes, int32_t put, double *V, void *stream) {
+    Layout L;
+    int rc = make_layout(b, L);
+    if (rc) return rc;
+    rc = check_ws(L, workspace, ws_bytes);
+    if (rc) return rc;
+    FDADI_REQUIRE(strikes && V && b->spots, "null payoff argument");
+    Arena A = arena_view(L, (char *)workspace);
+    payoff_kernel<<<(unsigned)L.n_tiles, EXPL_THREADS, 0, as_stream(stream)>>>(A, b->spots, strikes,
+                                                                               put ? 1 : 0, V);
     FDADI_CHECK_LAUNCH();
     return FDADI_OK;
 }

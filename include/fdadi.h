@@ -256,6 +256,14 @@ int fdadi_heston_tune(const fdadi_heston_batch_t *batch, void *workspace,
                       int64_t workspace_bytes, int32_t reps, fdadi_heston_plan_t *plan,
                       void *stream);
 
+/* Initial state of every option on its mesh, built on the device (the
+ * reference initializes the grid on the host, heston.py:402): V = max(S - K, 0)
+ * for calls (put == 0) or max(K - S, 0) for puts, with strikes DEVICE
+ * double [n_options] and V the packed arena. Requires a prepared workspace. */
+int fdadi_heston_payoff(const fdadi_heston_batch_t *batch, void *workspace,
+                        int64_t workspace_bytes, const double *strikes, int32_t put, double *V,
+                        void *stream);
+
 /* Per-option status words (the reference raises from DIE() on a failed solve,
  * common.h:17-27; a batch reports per option instead). */
 #define FDADI_STATUS_PIVOT 1      /* a line-solve pivot of the option was zero or non-finite */

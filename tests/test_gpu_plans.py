@@ -294,3 +294,19 @@ def test_minimum_and_ragged_grids_vs_oracle(cuda, plan, scheme):
         assert np.isfinite(out[k]).all(), sizes[k]
         assert _rel(out[k], ref) < 1e-11, (sizes[k], _rel(out[k], ref))
     assert not b.status(b.pack(out)).any()
+
+
+@pytest.mark.parametrize("put", [False, True])
+def test_device_payoff_matches_host_grid(uneven, put):
+    """The payoff built on the device equals the host-built initial grids bit
+    for bit."""
+    from fd_adi_gb300.batch import HestonBatch
+    opts, meshes, V0, ref, kw = uneven
+    b = HestonBatch(opts, meshes, **kw)
+    K = torch.tensor([o.strike for o in opts], dtype=torch.float64, device="cuda")
+    V = b.payoff(K, put=put)
+    torch.cuda.synchronize()
+    for k, (S, v) in enumerate(meshes):
+        want = (np.maximum(opts[k].strike - S, 0.0) if put else np.maximum(S - opts[k].strike, 0.0))
+        want = want[:, None] * np.ones((1, v.size))
+        np.testing.assert_array_equal(b.unpack(V)[k], want)
