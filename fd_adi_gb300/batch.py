@@ -241,7 +241,11 @@ class HestonBatch(object):
 
     def payoff(self, strikes, V=None, put=False):
         """Initial state built on the device: max(S - K, 0) (or the put's
-        max(K - S, 0)) on every option's mesh. strikes: device float64 [n]."""
+        max(K - S, 0)) on every option's mesh. strikes: device float64 [n].
+
+        The payoff is taken on the batch's own spots. The reference takes it
+        before a grid point is moved onto the spot (heston.py:402-406); for
+        that order, build the grids on the host and use pack()."""
         if V is None:
             V = torch.empty(self.total_points, dtype=torch.float64, device=self.device)
         cur = torch.cuda.current_stream(self.device)
