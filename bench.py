@@ -377,7 +377,16 @@ def run_surrogate(args):
     torch.cuda.synchronize()
     t_data = time.perf_counter() - t0
     adi_rate = (args.train + args.test) / t_data
-    sur = Surrogate(members=4, seed=args.seed, device=dev)
+    # the same data with the plain Black-Scholes control variate, for comparison
+    alt = {}
+    for cv in ([c for c in (0, 1, 2) if c != args.cv] if args.compare_cv else []):
+        s_alt = Surrogate(members=4, seed=args.seed, device=dev, cv=cv)
+        s_alt.fit(Qtr, ptr, dtr, epochs=args.epochs, batch=8192, lr=1e-3)
+        pa = s_alt.predict(torch.as_tensor(Qte, device=dev))[0].cpu().numpy()
+        alt["cv%d_heldout_rms_abs_err" % cv] = float(np.sqrt(np.mean((pa - pte) ** 2)))
+        alt["cv%d_heldout_max_abs_err" % cv] = float(np.abs(pa - pte).max())
+        del s_alt
+    sur = Surrogate(members=4, seed=args.seed, device=dev, cv=args.cv)
     t0 = time.perf_counter()
     sur.fit(Qtr, ptr, dtr, epochs=args.epochs, batch=8192, lr=1e-3)
     torch.cuda.synchronize()
@@ -452,6 +461,11 @@ def run_surrogate(args):
                           "query_rms_abs_err": float(np.sqrt(np.mean(qerr ** 2))),
                           "batched_adi_options_per_s": adi_rate,
                           "speedup_vs_batched_adi": value / adi_rate,
+                          "control_variate": ("Black-Scholes at mean variance" if args.cv == 0
+                                              else "Black-Scholes at mean variance + order-%d "
+                                              "series in vol of variance (price), residual / "
+                                              "(sigma sqrt T + 0.1)" % args.cv),
+                          **alt,
                           "data_gen_s": t_data, "train_s": t_train,
                           "forward_ms": fwd_ms}}
     print(json.dumps(line))
@@ -571,6 +585,11 @@ def main():
     ap.add_argument("--queries", type=int, default=100000)
     ap.add_argument("--epochs", type=int, default=50)
     ap.add_argument("--sample", type=int, default=2000)
+    ap.add_argument("--cv", type=int, default=0, choices=[0, 1, 2],
+                    help="surrogate control variate: 0 Black-Scholes at the mean variance, "
+                         "1 or 2 plus the vol-of-variance series to that order")
+    ap.add_argument("--compare-cv", action="store_true",
+                    help="also train on the same data with the other control variates")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))

@@ -1074,7 +1074,60 @@ __global__ void adam_kernel(float *p, const float *gr, float *m1, float *m2, int
 // inputs (8 of 16 columns; the rest zero); a Black-Scholes control variate at
 // the expected mean variance vbar = theta + (v0 - theta)(1 - e^{-kappa T})/(kappa T):
 // base = (price / K, delta); inbox = every feature inside the box.
-__global__ void featurize_kernel(const double *q, int M, const double *lo, const double *hi,
+// Heston call price around Black-Scholes at the expected total variance
+// W = theta T + (v0 - theta)(1 - e^{-kappa T}) / kappa, expanded in the
+// volatility of variance sigma (Lewis, "Option Valuation under Stochastic
+// Volatility", 2000, ch. 3):
+//   P = u(x, W) + rho sigma h1 u_xw                                  (order 1)
+//       + sigma^2 hA u_ww + rho^2 sigma^2 (hB u_xxw + hC u_xxww)     (order 2)
+// u(x, w) the Black-Scholes call in x = ln S and total variance w. Each h(v, t)
+// solves h_t - kappa (theta - v) h_v = (the term's source) with h(v, 0) = 0:
+// sources v b, v b^2 / 2, v h1_v and v h1 b (h1_v the coefficient of v in h1,
+// b = (1 - e^{-kappa t}) / kappa), which give the closed forms below
+// (h1, hA, hB linear in v, hC quadratic). Every derivative of u is
+// S phi(d1) times a polynomial in d1 and s = sqrt(w). Writes the first- and
+// second-order terms in price/K (c2 = 0 for order 1) and returns the price/K.
+__device__ double heston_series(double S, double K, double T, double r, double kap, double th,
+                                double sig, double rho, double v0, int order, double &c1,
+                                double &c2) {
+    const double kt = kap * T, em = exp(-kt), k2 = kap * kap, k3 = k2 * kap, k4 = k2 * k2;
+    const double W = th * T + (v0 - th) * (-expm1(-kt)) / kap;
+    const double s = sqrt(fmax(W, 1e-12));
+    const double d1 = (log(S / K) + r * T) / s + 0.5 * s, d2 = d1 - s;
+    const double N1 = 0.5 * erfc(-d1 * 0.7071067811865476);
+    const double N2 = 0.5 * erfc(-d2 * 0.7071067811865476);
+    const double Sphi = S * 0.3989422804014327 * exp(-0.5 * d1 * d1) / K;   // S phi(d1) / K
+    const double s2 = s * s, s3 = s2 * s, s5 = s3 * s2;
+    const double h1 = th * (kt + kt * em - 2.0 + 2.0 * em) / k2 + v0 * (1.0 - em - kt * em) / k2;
+    c1 = rho * sig * h1 * (-d2 / (2.0 * s2)) * Sphi;
+    c2 = 0.0;
+    if (order >= 2) {
+        const double kt2 = kt * kt, em2 = em * em;
+        const double hA = th * (2.0 * kt + 4.0 * (kt + 1.0) * em - 5.0 + em2) / (4.0 * k3) +
+                          v0 * (1.0 - em2 - 2.0 * kt * em) / (2.0 * k3);
+        const double hB = th * (kt2 * em + 2.0 * kt + 4.0 * kt * em - 6.0 + 6.0 * em) / (2.0 * k3) +
+                          v0 * (1.0 - em - kt * em - 0.5 * kt2 * em) / k3;
+        const double q0 = th * th *
+                          (kt2 + kt2 * em2 - 4.0 * kt + 4.0 * kt * em2 + 2.0 * (kt2 - 4.0) * em +
+                           4.0 + 4.0 * em2) / (2.0 * k4);
+        const double q1 = th * (-kt2 * em - kt2 * em2 + 2.0 * kt * em - 3.0 * kt * em2 +
+                                (kt - 2.0) + 4.0 * em - 2.0 * em2) / k4;
+        const double q2 = (kt2 * em2 + 2.0 * kt * em2 - 2.0 * kt * em + 1.0 - 2.0 * em + em2) /
+                          (2.0 * k4);
+        const double hC = q0 + v0 * (q1 + v0 * q2);
+        // u derivatives / (S phi(d1))
+        const double d12 = d1 * d1, d13 = d12 * d1, d14 = d13 * d1;
+        const double u_ww = (d1 * d2 - 1.0) / (4.0 * s3);
+        const double u_xxw = (d2 * d2 - 1.0) / (2.0 * s3);
+        const double u_xxww = (d14 - 3.0 * d13 * s + 3.0 * d12 * s2 - 6.0 * d12 - d1 * s3 +
+                               9.0 * d1 * s - 3.0 * s2 + 3.0) / (4.0 * s5);
+        const double rs2 = rho * sig * rho * sig;
+        c2 = (sig * sig * hA * u_ww + rs2 * (hB * u_xxw + hC * u_xxww)) * Sphi;
+    }
+    return (S / K) * N1 - exp(-r * T) * N2 + c1 + c2;
+}
+
+__global__ void featurize_kernel(const double *q, int M, const double *lo, const double *hi, int cv,
                                  bf16 *X, double *base, int *inbox) {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= M) return;
@@ -1094,21 +1147,33 @@ __global__ void featurize_kernel(const double *q, int M, const double *lo, const
     const double d1 = (log(S / K) + r * T) / sv + 0.5 * sv, d2 = d1 - sv;
     const double n1 = 0.5 * erfc(-d1 * 0.7071067811865476), n2 = 0.5 * erfc(-d2 * 0.7071067811865476);
     const double b0 = (S / K) * n1 - exp(-r * T) * n2;
-    base[2 * (int64_t)m] = b0;
-    base[2 * (int64_t)m + 1] = n1;
+    // the series corrects the price only: its delta leaves [0, 1] far out in
+    // the box, so the delta keeps the Black-Scholes variate
+    double price = b0, c1 = 0.0, c2 = 0.0, scale = 1.0;
+    if (cv > 0) {
+        price = heston_series(S, K, T, r, kap, th, p[6], p[7], v0, cv, c1, c2);
+        // the residual grows with sigma sqrt(T); the floor keeps error that
+        // does not (the ADI grid's own) from being magnified at small sigma
+        scale = p[6] * sqrt(T) + 0.1;
+    }
+    base[4 * (int64_t)m] = price;
+    base[4 * (int64_t)m + 1] = n1;
+    base[4 * (int64_t)m + 2] = scale;
+    base[4 * (int64_t)m + 3] = 1.0;
     // derived inputs (functions of the same 8 parameters), roughly in [-1, 1]:
-    // the control variate's price and delta, d1, total std, sqrt(T), mean variance
+    // the Black-Scholes price and delta, d1, total std, sqrt(T), mean variance
+    // and, for the series control variate, its first- and second-order terms
     const double g[8] = {4.0 * b0 - 1.0, 2.0 * n1 - 1.0, fmin(1.5, fmax(-1.5, d1 / 3.0)),
                          3.0 * sv - 1.0, 1.4142135623730951 * sqrt(T) - 1.0, 12.0 * vbar - 1.0,
-                         0.0, 0.0};
+                         fmin(1.5, fmax(-1.5, 40.0 * c1)), fmin(1.5, fmax(-1.5, 30.0 * c2))};
 #pragma unroll
     for (int k = 0; k < 8; ++k) X[(int64_t)m * 16 + 8 + k] = __float2bfloat16((float)g[k]);
 }
 
 // Ensemble read-out: member outputs y[p][m][0..1] (scaled residuals) ->
-// price = K (base0 + mean y0 / s0), delta = base1 + mean y1 / s1, spread =
-// max - min of the members' prices; fallback when out of the box or spread
-// > tol K.
+// price = K (base0 + base2 mean y0 / s0), delta = base1 + base3 mean y1 / s1,
+// spread = max - min of the members' prices; fallback when out of the box or
+// spread > tol K.
 __global__ void combine_kernel(const float *y, int64_t ldy, int64_t stride, int P, int M,
                                const double *q, const double *base, const int *inbox, double s0,
                                double s1, double tol, double *price, double *delta,
@@ -1119,9 +1184,9 @@ __global__ void combine_kernel(const float *y, int64_t ldy, int64_t stride, int 
     double sp = 0.0, sd = 0.0, mn = 1e300, mx = -1e300;
     for (int k = 0; k < P; ++k) {
         const float *row = y + k * stride + (int64_t)m * ldy;
-        const double pk = K * (base[2 * (int64_t)m] + (double)row[0] / s0);
+        const double pk = K * (base[4 * (int64_t)m] + base[4 * (int64_t)m + 2] * (double)row[0] / s0);
         sp += pk;
-        sd += base[2 * (int64_t)m + 1] + (double)row[1] / s1;
+        sd += base[4 * (int64_t)m + 1] + base[4 * (int64_t)m + 3] * (double)row[1] / s1;
         mn = fmin(mn, pk);
         mx = fmax(mx, pk);
     }
@@ -1411,10 +1476,11 @@ int fdadi_mlp_adam(float *p, const float *g, float *m1, float *m2, int64_t n, in
 }
 
 int fdadi_mlp_featurize(const double *queries, int32_t M, const double *lo, const double *hi,
-                        void *X, double *base, int32_t *inbox, void *stream) {
+                        int32_t cv, void *X, double *base, int32_t *inbox, void *stream) {
     FDADI_REQUIRE(queries && lo && hi && X && base && inbox && M > 0, "bad featurize arguments");
-    featurize_kernel<<<(M + 255) / 256, 256, 0, as_stream(stream)>>>(queries, M, lo, hi, (bf16 *)X,
-                                                                    base, inbox);
+    FDADI_REQUIRE(cv >= 0 && cv <= 2, "unknown control variate (0, 1 or 2)");
+    featurize_kernel<<<(M + 255) / 256, 256, 0, as_stream(stream)>>>(queries, M, lo, hi, cv,
+                                                                    (bf16 *)X, base, inbox);
     FDADI_CHECK_LAUNCH();
     return FDADI_OK;
 }

@@ -4,8 +4,11 @@ A 4-member ensemble of MLPs 8 -> 256 -> 256 -> 256 -> 256 -> 2 (SiLU) maps the
 Heston parameters (S0/K, T, r, kappa, theta, sigma, rho, v0) to price/K and
 delta. Each member learns the residual over a Black-Scholes control variate
 evaluated at the expected mean variance, which leaves the network a small,
-smooth correction. Weights and activations are bf16, accumulation and
-pre-activations fp32, master weights fp32 (Adam). Every layer of forward,
+smooth correction. (The featurizer also offers that price plus its first- or
+second-order expansion in the volatility of variance, cv = 1 or 2: a smaller
+residual, but on the same training data the network fits it worse, with
+larger held-out outliers, so cv = 0 is the default.) Weights and activations
+are bf16, accumulation and pre-activations fp32, master weights fp32 (Adam). Every layer of forward,
 backward and the weight update runs in libfdadi.so (tcgen05 tensor-core GEMMs
 with fused epilogues, include/fdadi.h); the four members are batched in every
 launch. Training data come from the batched FP64 ADI engine. Queries outside
@@ -185,20 +188,26 @@ class MLPEnsemble(object):
 
 class Featurizer(object):
     """Queries [M][9] (S0, K, T, r, kappa, theta, sigma, rho, v0) -> network
-    inputs, control variate and in-box flags, on the device."""
+    inputs, control variate [M][4] (price/K, delta, price-residual scale,
+    delta-residual scale) and in-box flags, on the device. cv = 0: the
+    Black-Scholes price at the expected mean variance; cv = 1 or 2: plus its
+    first- or second-order expansion in the volatility of variance."""
 
-    def __init__(self, device):
+    def __init__(self, device, cv=0):
+        if cv not in (0, 1, 2):
+            raise ValueError("unknown control variate %r (0, 1 or 2)" % (cv,))
         self.dev = device
+        self.cv = cv
         self.lo = torch.as_tensor(BOX_LO, device=device)
         self.hi = torch.as_tensor(BOX_HI, device=device)
 
     def __call__(self, Q):
         M = Q.shape[0]
         X = torch.empty(M, 16, dtype=torch.bfloat16, device=self.dev)
-        base = torch.empty(M, 2, dtype=torch.float64, device=self.dev)
+        base = torch.empty(M, 4, dtype=torch.float64, device=self.dev)
         inbox = torch.empty(M, dtype=torch.int32, device=self.dev)
-        _lib.call("fdadi_mlp_featurize", _p(Q), M, _p(self.lo), _p(self.hi), _p(X), _p(base),
-                  _p(inbox), _st())
+        _lib.call("fdadi_mlp_featurize", _p(Q), M, _p(self.lo), _p(self.hi), self.cv, _p(X),
+                  _p(base), _p(inbox), _st())
         return X, base, inbox
 
 
@@ -223,8 +232,7 @@ def adi_price(queries, nS=256, nv=128, nt=200, chunk=4096, graph=False, spot_max
         dts = qs[:, 2] / nt
         b = HestonBatch(params, ms, scheme="hv", n_steps=nt - 1, dt=dts, theta=HV_THETA,
                         implicit_steps=2, implicit_dt_factor=0.5, graph=graph)
-        V = b.pack([np.maximum(m[0][:, None] - r[1], 0.0) * np.ones((1, m[1].size))
-                    for m, r in zip(ms, qs)])
+        V = b.payoff(torch.as_tensor(qs[:, 1].copy(), device=b.device))
         b.run(V)
         idx = b.flat_index([(r[0], r[8]) for r in qs])
         vals = [b.gather(V, idx + off).cpu().numpy() for off in (-nv, 0, nv)]
@@ -261,10 +269,10 @@ def sobol_queries(n, seed=0, S0=100.0, lo=BOX_LO, hi=BOX_HI):
 class Surrogate(object):
     """Trained ensemble + control variate + fallback gate."""
 
-    def __init__(self, members=4, seed=0, device=None, tol=5e-4):
+    def __init__(self, members=4, seed=0, device=None, tol=5e-4, cv=0):
         self.dev = device or torch.device("cuda", torch.cuda.current_device())
         self.net = MLPEnsemble(members, seed, self.dev)
-        self.feat = Featurizer(self.dev)
+        self.feat = Featurizer(self.dev, cv)
         self.tol = tol
 
     def targets(self, Q, price, delta):
@@ -272,8 +280,8 @@ class Surrogate(object):
         Qd = torch.as_tensor(Q, device=self.dev)
         _, base, _ = self.feat(Qd)
         base = base.cpu().numpy()
-        r0 = price / Q[:, 1] - base[:, 0]
-        r1 = delta - base[:, 1]
+        r0 = (price / Q[:, 1] - base[:, 0]) / base[:, 2]
+        r1 = (delta - base[:, 1]) / base[:, 3]
         if not hasattr(self, "s"):
             self.s = (1.0 / max(np.std(r0), 1e-12), 1.0 / max(np.std(r1), 1e-12))
             self.net.scales = self.s

@@ -370,14 +370,17 @@ int fdadi_mlp_adam(float *p, const float *g, float *m1, float *m2, int64_t n, in
 
 /* Surrogate front end: queries [M][9] = (S0, K, T, r, kappa, theta, sigma,
  * rho, v0) -> bf16 network inputs X [M][16] (features S0/K, T, r, kappa,
- * theta, sigma, rho, v0 mapped to [-1, 1] by the box lo/hi [8]), the
- * Black-Scholes control variate base [M][2] = (price/K, delta) at the
- * expected mean variance, and inbox [M]. */
+ * theta, sigma, rho, v0 mapped to [-1, 1] by the box lo/hi [8], then derived
+ * inputs), the control variate base [M][4] = (price/K, delta, price-residual
+ * scale, delta-residual scale), and inbox [M]. cv = 0: Black-Scholes at the
+ * expected mean variance, scales 1. cv = 1 or 2: that price plus the first-
+ * or second-order expansion in the volatility of variance, price scale
+ * sigma sqrt(T) + 0.1 (the delta keeps the Black-Scholes variate). */
 int fdadi_mlp_featurize(const double *queries, int32_t M, const double *lo, const double *hi,
-                        void *X, double *base, int32_t *inbox, void *stream);
+                        int32_t cv, void *X, double *base, int32_t *inbox, void *stream);
 
 /* Ensemble read-out: y [problems][M][ldy] scaled residual outputs ->
- * price = K (base0 + mean y0 / s0), delta = base1 + mean y1 / s1, spread =
+ * price = K (base0 + base2 mean y0 / s0), delta = base1 + base3 mean y1 / s1, spread =
  * max - min of the members' prices, fallback = out of box or spread > tol*K;
  * *count += number of fallbacks. */
 int fdadi_mlp_combine(const float *y, int64_t ldy, int64_t stride, int32_t problems, int32_t M,
