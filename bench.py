@@ -372,11 +372,26 @@ def run_surrogate(args):
     t0 = time.perf_counter()
     Qtr = sobol_queries(args.train, seed=args.seed + 1)
     Qte = sobol_queries(args.test, seed=args.seed + 2)
-    ptr, dtr = adi_price(Qtr, pool=pool, **grid)
+    cached = None
+    if args.train_cache:
+        # training prices from an earlier run of the same pricer on the same
+        # seeded draws; the held-out set is still priced (and timed) here
+        d = np.load(args.train_cache)
+        if d["ptr"].shape != (args.train,):
+            raise SystemExit("--train-cache holds %d training prices, not %d"
+                             % (d["ptr"].shape[0], args.train))
+        ptr, dtr = d["ptr"], d["dtr"]
+        cached = "training prices loaded (%d draws, seed %d); held-out priced live" % (
+            args.train, args.seed + 1)
+        t0 = time.perf_counter()
+        n_priced = args.test
+    else:
+        ptr, dtr = adi_price(Qtr, pool=pool, **grid)
+        n_priced = args.train + args.test
     pte, dte = adi_price(Qte, pool=pool, **grid)
     torch.cuda.synchronize()
     t_data = time.perf_counter() - t0
-    adi_rate = (args.train + args.test) / t_data
+    adi_rate = n_priced / t_data
     # the same data with the plain Black-Scholes control variate, for comparison
     alt = {}
     for cv in ([c for c in (0, 1, 2) if c != args.cv] if args.compare_cv else []):
@@ -466,6 +481,8 @@ def run_surrogate(args):
                                               "series in vol of variance (price), residual / "
                                               "(sigma sqrt T + 0.1)" % args.cv),
                           **alt,
+                          "adam_betas": list(sur.net.adam[:2]),
+                          "train_data": cached or "priced in this run",
                           "data_gen_s": t_data, "train_s": t_train,
                           "forward_ms": fwd_ms}}
     print(json.dumps(line))
@@ -588,6 +605,9 @@ def main():
     ap.add_argument("--cv", type=int, default=0, choices=[0, 1, 2],
                     help="surrogate control variate: 0 Black-Scholes at the mean variance, "
                          "1 or 2 plus the vol-of-variance series to that order")
+    ap.add_argument("--train-cache", default=None,
+                    help="npz with the training set's ADI prices (ptr, dtr) from an earlier "
+                         "run on the same seeds")
     ap.add_argument("--compare-cv", action="store_true",
                     help="also train on the same data with the other control variates")
     args = ap.parse_args()

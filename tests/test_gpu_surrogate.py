@@ -94,6 +94,9 @@ def test_surrogate_learns_adi_prices_and_gates(dev):
     t_adi = (time.perf_counter() - t0) / Qtr.shape[0]
     pte, dte = adi_price(Qte, **grid)
     sur = Surrogate(members=4, seed=0, device=dev)
+    # 320 steps: too short for the default's 100-step moment averages, which
+    # suit the 6400-step full training; the classic constants fit here
+    sur.net.adam = (0.9, 0.999, 1e-8)
     losses = sur.fit(Qtr, ptr, dtr, epochs=40, batch=512, lr=2e-3)
     assert losses[-1] < 0.2 * losses[0]
     Q = torch.as_tensor(Qte, device=dev)
