@@ -48,9 +48,13 @@ STAGE_BYTES = {"explicit_hv0": 32, "explicit_hv3": 40, "spot_solve": 24, "var_so
                "var_solve_v": 16, "explicit_implicit": 16, "var_solve_implicit": 16,
                "spot_solve_implicit": 16}
 # DRAM bytes per grid point per launch measured by ncu (--set full) on the
-# 256-option cut of the batch workload (profiles/explicit_hv_batch256.md);
-# traffic grows with the points processed, so a full launch is this x points.
-NCU_TRAFFIC_B_PER_POINT = {"explicit_hv0": 52.7, "explicit_hv3": 62.3}
+# 256-option cut of the batch workload (profiles/explicit_hv_batch256.md and
+# profiles/line_solves_batch256.md); its state, operators and Thomas factors
+# already exceed L2, and traffic grows with the points processed, so a full
+# launch is this x points. The spot solve's figure includes its three Thomas
+# factors per point and the forward sweep's result read back by the backward
+# sweep, which the algorithmic state bytes leave out.
+NCU_TRAFFIC_B_PER_POINT = {"explicit_hv0": 52.7, "explicit_hv3": 62.3, "spot_solve": 56.9}
 # FP64 pipe work per grid point: FP64 instructions x 2, so that a pipe fully
 # busy with DFMA (2 flops each; DMUL and DADD occupy it the same) reads as the
 # DFMA peak that fdadi_fp64_probe measures. The mixed-term row sums are formed
@@ -773,6 +777,11 @@ def main():
                                   for k, v in st.items()},
                "stage_fp64_frac": {k: round(STAGE_FLOPS[k] * P / (v[0] * 1e-3) / 1e12 / fp64, 4)
                                    for k, v in st.items()},
+               # DRAM traffic (ncu bytes per point x points / launch time)
+               # against the HBM copy peak, where a traffic figure exists
+               "stage_dram_frac": {k: round(NCU_TRAFFIC_B_PER_POINT[k] * P / (v[0] * 1e-3) / 1e9
+                                            / hbm_peak, 4)
+                                   for k, v in st.items() if k in NCU_TRAFFIC_B_PER_POINT},
                "plan": dict(batch.plan, tuned=not (args.no_tune or args.plan),
                             setup_s=round(t_tune, 2)),
                "clocks": clk}
