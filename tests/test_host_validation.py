@@ -147,3 +147,17 @@ def test_gemm_and_inference_shape_errors():
     net.N[2] = 256
     assert lib.fdadi_mlp_infer(ctypes.byref(net), FAKE, 200, FAKE, None, None) == 1
     assert "multiple of 128" in _lib.last_error()
+
+
+def test_payoff_and_featurize_arguments():
+    lib = _lib.load()
+    b, keep = _batch([32, 40], [16, 20])
+    need = lib.fdadi_heston_workspace_bytes(ctypes.byref(b))
+    rc = lib.fdadi_heston_payoff(ctypes.byref(b), ctypes.c_void_p(FAKE), need, None, 0,
+                                 ctypes.c_void_p(FAKE), None)
+    assert rc == 1 and "null payoff argument" in _lib.last_error()
+    rc = lib.fdadi_heston_payoff(ctypes.byref(b), ctypes.c_void_p(FAKE), need - 256,
+                                 ctypes.c_void_p(FAKE), 0, ctypes.c_void_p(FAKE), None)
+    assert rc == 3 and "workspace too small" in _lib.last_error()
+    rc = lib.fdadi_mlp_featurize(FAKE, 128, FAKE, FAKE, 5, FAKE, FAKE, FAKE, None)
+    assert rc == 1 and "control variate" in _lib.last_error()
