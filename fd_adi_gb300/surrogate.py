@@ -92,8 +92,9 @@ class MLPEnsemble(object):
         # beta1, beta2, eps. Trained on 2^20 ADI-priced draws (50 epochs, batch
         # 8192, lr 1e-3 cosine), the held-out RMS price error is 0.0028 with
         # the usual (0.9, 0.999), 0.0020 with beta2 = 0.99 and 0.0016 with
-        # (0.99, 0.99): the fit is optimiser-limited (training error is no
-        # lower than held-out), and the long averages steady it.
+        # (0.99, 0.99). The error on training draws equals the held-out error
+        # in both cases, so the fit is the limit, not overfitting; the long
+        # moment averages steady the steps.
         self.adam = (0.99, 0.99, 1e-8)
 
     # -- buffers --
