@@ -86,7 +86,7 @@ def workload(n_options, seed, nt=200):
                 nS=nS.astype(np.int32), nv=nv.astype(np.int32), nt=nt)
 
 
-def workload_config2():
+def workload_large():
     """The large single-instance configuration: rho = -0.7, sigma = 0.5,
     K in {80, 100, 120} (one option each, run as one batch), 1024 x 512 grid,
     nt = 1000, HV theta = 1/2 + sqrt(3)/6 after two implicit half-steps."""
@@ -254,7 +254,7 @@ def stage_times(batch, V, torch):
 
 
 def plain_vs_batched(torch, n_batch=2048):
-    """Config 1 (150x150, nt=150: two implicit half-steps then Douglas 0.5):
+    """The 150x150 option (nt=150: two implicit half-steps then Douglas 0.5):
     options/s of the per-operator engine (the reference's per-step call
     sequence, one option per launch chain) vs the fused batched engine."""
     from fd_adi_gb300 import HestonOption, HestonFiniteDifferenceEngine, mesh
@@ -546,10 +546,10 @@ def cpu_baseline(w, n_sample, nt_sample=None):
 def run_reference(args, rank, world):
     if rank != 0:
         return 0
-    w = workload_config2() if args.workload == "config2" else workload(args.options, args.seed)
+    w = workload_large() if args.workload == "large" else workload(args.options, args.seed)
     rates = []
     for s in range(args.warmup + args.steps):
-        cb = cpu_baseline(w, args.ref_sample, 20 if args.workload == "config2" else None)
+        cb = cpu_baseline(w, args.ref_sample, 20 if args.workload == "large" else None)
         if s >= args.warmup:
             rates.append(cb["value"])
     value = float(np.mean(rates))
@@ -569,7 +569,7 @@ def run_reference(args, rank, world):
 
 
 def config_block(args, w):
-    if args.workload == "config2":
+    if args.workload == "large":
         return {"workload": "large single instance x3: K in {80,100,120}, 1024x512, nt=1000, "
                             "HV theta=1/2+sqrt(3)/6 with Rannacher start, rho=-0.7, sigma=0.5",
                 "options_per_gpu": int(len(w["K"])), "nt": int(w["nt"]),
@@ -600,7 +600,7 @@ def main():
                     help="line-solve launch plan from the size heuristic, not the autotuner")
     ap.add_argument("--plan", default=None,
                     help="launch plan as JSON (fdadi_heston_plan_t fields) instead of tuning")
-    ap.add_argument("--workload", default="batch", choices=["batch", "config2", "surrogate", "gemm"])
+    ap.add_argument("--workload", default="batch", choices=["batch", "large", "surrogate", "gemm"])
     ap.add_argument("--train", type=int, default=1 << 17)
     ap.add_argument("--test", type=int, default=1 << 13)
     ap.add_argument("--queries", type=int, default=100000)
@@ -639,7 +639,7 @@ def main():
     # weak scaling: the seeded workload has args.options options per rank and
     # is partitioned across ranks by work (no data-path collective)
     from fd_adi_gb300.shard import shard_of
-    w_all = (workload_config2() if args.workload == "config2"
+    w_all = (workload_large() if args.workload == "large"
              else workload(args.options * world, args.seed))
     mine = shard_of(w_all["nS"].astype(np.int64) * w_all["nv"], rank, world)
     w = subset(w_all, mine)
@@ -787,7 +787,7 @@ def main():
                "clocks": clk}
         if args.cpu_sample > 0:
             out["cpu_baseline"] = cpu_baseline(
-                w, args.cpu_sample, 20 if args.workload == "config2" else None)
+                w, args.cpu_sample, 20 if args.workload == "large" else None)
         if not args.no_extras:
             out["plain_vs_batched"] = plain_vs_batched(torch)
     if world > 1:

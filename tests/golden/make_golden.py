@@ -134,8 +134,8 @@ def solves():
     np.savez_compressed(os.path.join(HERE, "solves.npz"), **out)
 
 
-def config1():
-    """Config 1: 150x150, nt=150, two implicit half-steps then Douglas theta=0.5."""
+def heston150():
+    """150x150, nt=150, two implicit half-steps then Douglas theta=0.5."""
     S, v = H.heston_mesh(100., 100., 0.04, 150, 150, 800., 5.)
     F = H.heston_engine(100., 100., 0.06, 0.04, 1.0, 0.04, 0.2, 0.0, S, v)
     V0 = F.grid.domain[-1].copy()
@@ -143,12 +143,12 @@ def config1():
     V = H.quiet(F.solve_implicit, 2, dt * 0.5, initial=V0)
     V = H.quiet(F.solve_douglas, n - 1, dt, initial=V, theta=0.5)
     idx = H.price_index(S, v, 100., 0.04)
-    np.savez_compressed(os.path.join(HERE, "config1.npz"), S=S, v=v, V=V,
+    np.savez_compressed(os.path.join(HERE, "heston150.npz"), S=S, v=v, V=V,
                         price=np.array(V[idx]), idx=np.array(idx))
 
 
-def config2_short():
-    """Config 2 shape (1024x512, rho=-0.7, sigma=0.5, K=100, HV theta=1/2+sqrt(3)/6
+def heston1024x512_short():
+    """The large single grid (1024x512, rho=-0.7, sigma=0.5, K=100, HV theta=1/2+sqrt(3)/6
     after two implicit half-steps), shortened to 3 HV steps of dt=1/1000 so the
     reference finishes in seconds. Stores the price, a down-sampled grid and
     whole-grid checksums."""
@@ -159,7 +159,7 @@ def config2_short():
     V = H.quiet(F.solve_implicit, 2, dt * 0.5, initial=V0)
     V = H.quiet(F.solve_hundsdorferverwer, 3, dt, initial=V, theta=HV_THETA)
     idx = H.price_index(S, v, 100., 0.04)
-    np.savez_compressed(os.path.join(HERE, "config2_short.npz"), S=S, v=v,
+    np.savez_compressed(os.path.join(HERE, "heston1024x512_short.npz"), S=S, v=v,
                         V_sub=V[::16, ::8], price=np.array(V[idx]), idx=np.array(idx),
                         sum=np.array(V.sum()), sumsq=np.array((V * V).sum()),
                         rowsum=V.sum(axis=1), colsum=V.sum(axis=0))
@@ -194,8 +194,8 @@ if __name__ == "__main__":
     meshes()
     operators()
     solves()
-    config1()
-    config2_short()
+    heston150()
+    heston1024x512_short()
     blackscholes()
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):

@@ -1,6 +1,6 @@
 """CUDA path against the oracle and the reference's golden outputs.
 
-Tolerances: the spec bar is price within 1e-10 relative and the full
+Tolerances: the parity bar is price within 1e-10 relative and the full
 grid within 1e-9 max-norm of the reference CPU engine; on the small fixtures
 the fused kernels agree to ~1e-13 relative, so those tests use 1e-11 of the
 grid's max to catch semantic slips early.
@@ -68,11 +68,11 @@ def test_fused_batch_vs_golden(cuda, golden, scheme):
         assert _rel(out[k], orc) < 1e-11, keys[i]
 
 
-def test_config1_price_and_grid(cuda, golden):
+def test_heston150_price_and_grid(cuda, golden):
     """150x150, nt=150: two implicit half-steps then Douglas theta=0.5."""
     from fd_adi_gb300.batch import HestonBatch, payoff_grids
     from fd_adi_gb300 import HestonOption
-    g = golden("config1")
+    g = golden("heston150")
     opt = HestonOption(spot=100., strike=100., interest_rate=0.06, volatility=0.2, tenor=1.0,
                        mean_reversion=1.0, mean_variance=0.04, vol_of_variance=0.2,
                        correlation=0.0)
@@ -92,10 +92,10 @@ def test_config1_price_and_grid(cuda, golden):
     assert p == V[idx]
 
 
-def test_config2_shape_vs_reference(cuda, golden):
+def test_heston1024x512_shape_vs_reference(cuda, golden):
     """1024x512, rho=-0.7, sigma=0.5: 2 implicit half-steps + 3 HV steps."""
     from fd_adi_gb300.batch import HestonBatch
-    g = golden("config2_short")
+    g = golden("heston1024x512_short")
     S, v = g["S"], g["v"]
     V0 = np.maximum(S[:, None] - 100.0, 0) * np.ones((1, v.size))
     dt = 1.0 / 1000
@@ -138,7 +138,7 @@ def test_uneven_batch_vs_oracle(cuda):
     for k in range(16):
         # coarse grids with long steps amplify rounding near S_max: the oracle
         # itself is 3e-10 (relative to max-norm) from the reference on option
-        # 0 while prices agree to 1e-12, so the spec bars apply here
+        # 0 while prices agree to 1e-12, so the parity bars apply here
         assert _rel(out[k], ref[k]) < 1e-9, k
         i, j = M.price_index(meshes[k][0], meshes[k][1], 100., opts[k].variance.value)
         assert abs(out[k][i, j] - ref[k][i, j]) <= 1e-10 * abs(ref[k][i, j]), k
@@ -265,7 +265,7 @@ def test_blackscholes_engine(cuda, golden):
         assert _rel(fn(), g[name]) < 1e-11, name
 
 
-def test_linearity_at_config2_size(cuda):
+def test_linearity_at_1024x512(cuda):
     """Size-independent property at 1024x512: the scheme is linear in the
     initial grid apart from the boundary residual, so
     solve(a U + b W) - solve(0) = a (solve(U) - solve(0)) + b (solve(W) - solve(0))."""

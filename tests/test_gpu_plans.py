@@ -2,7 +2,7 @@
 and the reference's golden outputs, and the autotuner.
 
 The partitioned spot solve and the pipelined variance solve reassociate the
-Thomas recurrences, so they are held to the spec bars (price within
+Thomas recurrences, so they are held to the parity bars (price within
 1e-10 relative, grid within 1e-9 of its max-norm), not bit equality.
 """
 import numpy as np
@@ -133,12 +133,12 @@ def test_unknown_plan_is_rejected(uneven):
 
 @pytest.mark.parametrize("plan", [((1, 32, 32), (1, 4)), ((1, 8, 128), (1, 1)),
                                   ((0, 8, 32), (1, 2))])
-def test_config1_golden_with_plan(cuda, golden, plan):
-    """Config 1 (150x150, 2 implicit half-steps + Douglas) against the
+def test_heston150_golden_with_plan(cuda, golden, plan):
+    """The 150x150 option (2 implicit half-steps + Douglas) against the
     reference's golden output under partitioned and pipelined plans."""
     from fd_adi_gb300.batch import HestonBatch, payoff_grids, make_plan
     from fd_adi_gb300 import HestonOption
-    g = golden("config1")
+    g = golden("heston150")
     opt = HestonOption(spot=100., strike=100., interest_rate=0.06, volatility=0.2, tenor=1.0,
                        mean_reversion=1.0, mean_variance=0.04, vol_of_variance=0.2,
                        correlation=0.0)
@@ -153,11 +153,11 @@ def test_config1_golden_with_plan(cuda, golden, plan):
 
 
 @pytest.mark.parametrize("var", [(1, 2), (3, 16), (3, 4)])
-def test_config2_golden_partitioned(cuda, golden, var):
+def test_heston1024x512_golden_partitioned(cuda, golden, var):
     """1024x512 (long lines: the partitioned solves' case) against the
     reference's golden output."""
     from fd_adi_gb300.batch import HestonBatch, make_plan
-    g = golden("config2_short")
+    g = golden("heston1024x512_short")
     S, v = g["S"], g["v"]
     V0 = np.maximum(S[:, None] - 100.0, 0) * np.ones((1, v.size))
     b = HestonBatch([(0.06, 1.0, 0.04, 0.5, -0.7)], [(S, v)], scheme="hv", n_steps=3,
@@ -251,7 +251,7 @@ def test_greeks_match_host_stencils(uneven):
         assert p[k] == out[k][i, j]
         assert abs(d[k] - np.dot(w1, col)) <= 1e-12 * max(1.0, abs(d[k]))
         assert abs(g[k] - np.dot(w2, col)) <= 1e-10 * max(1.0, abs(g[k]))
-        # against the oracle's grid: the spec price bar, delta alike
+        # against the oracle's grid: the parity price bar, delta alike
         cr = ref[k][i - 1:i + 2, j]
         assert abs(d[k] - np.dot(w1, cr)) <= 1e-9 * max(1.0, abs(d[k]))
 

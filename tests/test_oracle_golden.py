@@ -57,21 +57,21 @@ def test_solves_match_reference(golden, case):
     assert np.abs(out - ref).max() <= 1e-12 * scale, key
 
 
-def test_config1_full_grid(golden):
-    g = golden("config1")
+def test_heston150_full_grid(golden):
+    g = golden("heston150")
     S, v = g["S"], g["v"]
     V0 = np.maximum(S[:, None] - 100.0, 0) * np.ones((1, v.size))
     n, dt = 150, 1.0 / 150
     out = O.heston_solve(S, v, 0.06, 1.0, 0.04, 0.2, 0.0, V0,
                          [("implicit", 2, dt * 0.5, 1.0), ("douglas", n - 1, dt, 0.5)])
     idx = tuple(g["idx"])
-    # spec tolerances: price 1e-10 relative, grid 1e-9 max-norm
+    # parity tolerances: price 1e-10 relative, grid 1e-9 max-norm
     assert abs(out[idx] - g["price"]) <= 1e-10 * abs(g["price"])
     assert np.abs(out - g["V"]).max() <= 1e-9 * np.abs(g["V"]).max()
 
 
-def test_config1_vs_semianalytic(golden):
-    g = golden("config1")
+def test_heston150_vs_semianalytic(golden):
+    g = golden("heston150")
     cos = analytic.heston_cos(100., 100., 0.06, 0.04, 1.0, 1.0, 0.04, 0.2, 0.0)[0, 0]
     # the reference's own accuracy bar (tests/test_HestonOptionGPU.py: rtol 1e-3)
     assert abs(float(g["price"]) - cos) <= 1e-3 * cos
