@@ -246,8 +246,16 @@ class HestonBatch(object):
         The payoff is taken on the batch's own spots. The reference takes it
         before a grid point is moved onto the spot (heston.py:402-406); for
         that order, build the grids on the host and use pack()."""
+        if (strikes.dtype != torch.float64 or not strikes.is_cuda or strikes.numel() != self.n
+                or not strikes.is_contiguous()):
+            raise ValueError("strikes must be a contiguous CUDA float64 tensor of %d values"
+                             % self.n)
         if V is None:
             V = torch.empty(self.total_points, dtype=torch.float64, device=self.device)
+        elif (V.dtype != torch.float64 or not V.is_cuda or V.numel() != self.total_points
+              or not V.is_contiguous()):
+            raise ValueError("state must be a contiguous CUDA float64 tensor of %d points"
+                             % self.total_points)
         cur = torch.cuda.current_stream(self.device)
         _lib.call("fdadi_heston_payoff", ctypes.byref(self.struct),
                   ctypes.c_void_p(self.workspace.data_ptr()), self.workspace_bytes,

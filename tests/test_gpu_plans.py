@@ -310,3 +310,17 @@ def test_device_payoff_matches_host_grid(uneven, put):
         want = (np.maximum(opts[k].strike - S, 0.0) if put else np.maximum(S - opts[k].strike, 0.0))
         want = want[:, None] * np.ones((1, v.size))
         np.testing.assert_array_equal(b.unpack(V)[k], want)
+
+
+def test_device_payoff_rejects_bad_arguments(uneven):
+    """Strikes and state are checked before the launch: wrong length, dtype
+    or device raise ValueError instead of reading or writing out of bounds."""
+    from fd_adi_gb300.batch import HestonBatch
+    opts, meshes, V0, ref, kw = uneven
+    b = HestonBatch(opts, meshes, **kw)
+    K = torch.tensor([o.strike for o in opts], dtype=torch.float64, device="cuda")
+    for bad in (K[:-1], K.float(), K.cpu()):
+        with pytest.raises(ValueError):
+            b.payoff(bad)
+    with pytest.raises(ValueError):
+        b.payoff(K, torch.empty(b.total_points - 1, dtype=torch.float64, device="cuda"))
