@@ -226,10 +226,23 @@ class HestonBatch(object):
         return [h[self.p_off[k]:self.p_off[k + 1]].reshape(self.n0[k], self.n1[k])
                 for k in range(self.n)]
 
+    def _check_state(self, V):
+        """The kernels index V by the arena's offsets: refuse anything else."""
+        if (V.dtype != torch.float64 or not V.is_cuda or V.numel() != self.total_points
+                or not V.is_contiguous()):
+            raise ValueError("state must be a contiguous CUDA float64 tensor of %d points"
+                             % self.total_points)
+
+    @staticmethod
+    def _check_index(idx, n=None):
+        if (idx.dtype != torch.int64 or not idx.is_cuda or not idx.is_contiguous()
+                or (n is not None and idx.numel() != n)):
+            raise ValueError("indices must be a contiguous CUDA int64 tensor%s"
+                             % ("" if n is None else " of %d values" % n))
+
     def run(self, V):
         """Advance the packed state arena V (device, float64) in place."""
-        if V.dtype != torch.float64 or not V.is_cuda or V.numel() != self.total_points:
-            raise ValueError("state must be a CUDA float64 tensor of %d points" % self.total_points)
+        self._check_state(V)
         if self.graph:
             self.stream.wait_stream(torch.cuda.current_stream(self.device))
         _lib.call("fdadi_heston_run", ctypes.byref(self.struct),
@@ -252,10 +265,7 @@ class HestonBatch(object):
                              % self.n)
         if V is None:
             V = torch.empty(self.total_points, dtype=torch.float64, device=self.device)
-        elif (V.dtype != torch.float64 or not V.is_cuda or V.numel() != self.total_points
-              or not V.is_contiguous()):
-            raise ValueError("state must be a contiguous CUDA float64 tensor of %d points"
-                             % self.total_points)
+        self._check_state(V)
         cur = torch.cuda.current_stream(self.device)
         _lib.call("fdadi_heston_payoff", ctypes.byref(self.struct),
                   ctypes.c_void_p(self.workspace.data_ptr()), self.workspace_bytes,
@@ -266,6 +276,8 @@ class HestonBatch(object):
     def greeks(self, V, flat_idx):
         """(price, delta, gamma) device tensors: each option's value at its
         arena index and the centred non-uniform S-derivatives there."""
+        self._check_state(V)
+        self._check_index(flat_idx, self.n)
         out = [torch.empty(self.n, dtype=torch.float64, device=self.device) for _ in range(3)]
         cur = torch.cuda.current_stream(self.device)
         _lib.call("fdadi_heston_greeks", ctypes.byref(self.struct),
@@ -278,6 +290,7 @@ class HestonBatch(object):
         """Per-option status words (numpy int32): bit 1 = a line-solve pivot
         was zero or non-finite when the operators were built, bit 2 = the
         option's grid in V holds a NaN or infinity."""
+        self._check_state(V)
         out = torch.empty(self.n, dtype=torch.int32, device=self.device)
         with torch.cuda.stream(self.stream):
             _lib.call("fdadi_heston_status", ctypes.byref(self.struct),
@@ -330,6 +343,10 @@ class HestonBatch(object):
         return torch.as_tensor(idx, device=self.device)
 
     def gather(self, V, flat_idx, out=None):
+        """V[flat_idx] on the device (the price read-out); flat_idx are arena
+        indices as flat_index() returns them."""
+        self._check_state(V)
+        self._check_index(flat_idx)
         if out is None:
             out = torch.empty(flat_idx.numel(), dtype=torch.float64, device=self.device)
         _lib.call("fdadi_gather", ctypes.c_void_p(V.data_ptr()),

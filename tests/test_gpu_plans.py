@@ -312,9 +312,10 @@ def test_device_payoff_matches_host_grid(uneven, put):
         np.testing.assert_array_equal(b.unpack(V)[k], want)
 
 
-def test_device_payoff_rejects_bad_arguments(uneven):
-    """Strikes and state are checked before the launch: wrong length, dtype
-    or device raise ValueError instead of reading or writing out of bounds."""
+def test_batch_rejects_bad_arguments(uneven):
+    """State, strikes and index tensors are checked before any launch: a wrong
+    length, dtype or device raises ValueError instead of reading or writing
+    out of bounds."""
     from fd_adi_gb300.batch import HestonBatch
     opts, meshes, V0, ref, kw = uneven
     b = HestonBatch(opts, meshes, **kw)
@@ -322,5 +323,17 @@ def test_device_payoff_rejects_bad_arguments(uneven):
     for bad in (K[:-1], K.float(), K.cpu()):
         with pytest.raises(ValueError):
             b.payoff(bad)
-    with pytest.raises(ValueError):
-        b.payoff(K, torch.empty(b.total_points - 1, dtype=torch.float64, device="cuda"))
+    V = b.pack(V0)
+    idx = b.flat_index()
+    strided = torch.empty(2 * b.total_points, dtype=torch.float64, device="cuda")[::2]
+    for badV in (V[:-1], V.float(), V.cpu(), strided):
+        for call in (lambda: b.payoff(K, badV), lambda: b.run(badV), lambda: b.status(badV),
+                     lambda: b.greeks(badV, idx), lambda: b.gather(badV, idx)):
+            with pytest.raises(ValueError):
+                call()
+    for bad in (idx[:-1], idx.int(), idx.cpu()):
+        with pytest.raises(ValueError):
+            b.greeks(V, bad)
+    for bad in (idx.int(), idx.cpu()):
+        with pytest.raises(ValueError):
+            b.gather(V, bad)
