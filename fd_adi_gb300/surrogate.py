@@ -210,6 +210,9 @@ class Featurizer(object):
         self.hi = torch.as_tensor(BOX_HI, device=device)
 
     def __call__(self, Q):
+        if (Q.dtype != torch.float64 or not Q.is_cuda or Q.dim() != 2 or Q.shape[1] != 9
+                or not Q.is_contiguous()):
+            raise ValueError("queries must be a contiguous CUDA float64 tensor [M][9]")
         M = Q.shape[0]
         X = torch.empty(M, 16, dtype=torch.bfloat16, device=self.dev)
         base = torch.empty(M, 4, dtype=torch.float64, device=self.dev)
@@ -323,6 +326,7 @@ class Surrogate(object):
     def predict(self, Q):
         """Q: [n][9] device float64. Returns (price, delta, spread, fallback
         flags, fallback count) on the device."""
+        Q = Q.contiguous()      # featurize and combine both read it as [n][9]
         M0 = Q.shape[0]
         M = ((M0 + 127) // 128) * 128
         if M != M0:

@@ -204,7 +204,13 @@ def test_series_control_variate_across_the_box(dev):
         np.testing.assert_array_equal(b[cv][:, 3], 1.0)
 
 
-def test_unknown_control_variate_is_rejected(dev):
+def test_unknown_control_variate_and_bad_queries_are_rejected(dev):
     from fd_adi_gb300.surrogate import Featurizer
     with pytest.raises(ValueError):
         Featurizer(dev, 3)
+    f = Featurizer(dev)
+    Q = torch.ones(256, 9, dtype=torch.float64, device=dev)
+    for bad in (Q.float(), Q.cpu(), Q[:, :8], torch.ones(256, 18, dtype=torch.float64,
+                                                          device=dev)[:, ::2]):
+        with pytest.raises(ValueError):
+            f(bad)
