@@ -21,10 +21,19 @@
  * flattened order after rolling the operator's axis last,
  * BandedOperator.pyx:335-337).
  */
+#include <malloc.h>
 #include <math.h>
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
+
+/* Every apply and solve takes grid-sized scratch from malloc; keep those
+ * blocks on the heap (glibc would map and unmap each one, paying page faults
+ * on every call). */
+__attribute__((constructor)) static void oracle_malloc_tuning(void) {
+    mallopt(M_MMAP_THRESHOLD, 256 << 20);
+    mallopt(M_TRIM_THRESHOLD, 512 << 20);
+}
 
 enum { CANNOT_FOLD = 0, CAN_FOLD = 1, FOLDED = 2 };
 enum { BND_NONE = -1, BND_DIRICHLET = 0, BND_NEUMANN = 1 };
@@ -274,8 +283,13 @@ static void fold_vector(const op_t *o, double *v, int unfold) {
 /* Grid V has shape [n0][n1] row-major (n1 = 1 for one dimension). An axis-0
  * operator sees line b = column j, element k = row i; an axis-1 operator sees
  * line b = row i, element k = column j (BandedOperator.pyx:335-337). */
+/* Lines are independent within every loop below, so large grids spread them
+ * over threads (each element's arithmetic is unchanged, and so are the bits);
+ * inside oracle_heston_batch's per-option threads these run single-threaded. */
+#define PAR_MIN 65536
 static void gather(const op_t *o, const double *V, int n0, int n1, double *flat) {
     if (o->axis == 0) {
+#pragma omp parallel for if ((long)n0 * n1 >= PAR_MIN)
         for (int j = 0; j < n1; ++j)
             for (int i = 0; i < n0; ++i) flat[j * n0 + i] = V[i * n1 + j];
     } else {
@@ -285,6 +299,7 @@ static void gather(const op_t *o, const double *V, int n0, int n1, double *flat)
 
 static void scatter(const op_t *o, const double *flat, int n0, int n1, double *V) {
     if (o->axis == 0) {
+#pragma omp parallel for if ((long)n0 * n1 >= PAR_MIN)
         for (int j = 0; j < n1; ++j)
             for (int i = 0; i < n0; ++i) V[i * n1 + j] = flat[j * n0 + i];
     } else {
@@ -307,6 +322,7 @@ static void op_apply(const op_t *o, const double *V, int n0, int n1, double *out
     double *y = (double *)malloc((size_t)N * sizeof(double));
     if (o->mixed) {
         memcpy(x, V, (size_t)N * sizeof(double));
+#pragma omp parallel for if (N >= PAR_MIN)
         for (int i = 0; i < n0; ++i)
             for (int j = 0; j < n1; ++j) {
                 const double *c = o->m9 + (size_t)(i * n1 + j) * 9;
@@ -329,6 +345,7 @@ static void op_apply(const op_t *o, const double *V, int n0, int n1, double *out
     gather(o, V, n0, n1, x);
     force_dirichlet(o, x);
     int L = o->L;
+#pragma omp parallel for if (N >= PAR_MIN)
     for (int b = 0; b < o->blocks; ++b) {
         for (int k = 0; k < L; ++k) {
             int i = b * L + k;
@@ -367,7 +384,10 @@ static void op_solve(const op_t *o_in, double *V, int n0, int n1) {
         o = tmp;
     }
     if (op_folded(o)) fold_vector(o, x, 0);
+#pragma omp parallel if (N >= PAR_MIN)
+    {
     double *cp = (double *)malloc((size_t)L * sizeof(double));
+#pragma omp for
     for (int b = 0; b < o->blocks; ++b) {
         double *r = x + (size_t)b * L;
         const double *sup = o->d[1] + (size_t)b * L, *mid = o->d[2] + (size_t)b * L,
@@ -382,6 +402,7 @@ static void op_solve(const op_t *o_in, double *V, int n0, int n1) {
         for (int k = L - 2; k >= 0; --k) r[k] = r[k] - cp[k] * r[k + 1];
     }
     free(cp);
+    }
     scatter(o, x, n0, n1, V);
     free(x);
     if (tmp) op_free(tmp);
@@ -479,8 +500,14 @@ static void bs_engine(engine_t *E, const double *S, int nS, double r, double var
     free(vec);
 }
 
-static void vadd(double *a, const double *b, size_t n) { for (size_t i = 0; i < n; ++i) a[i] += b[i]; }
-static void vsub(double *a, const double *b, size_t n) { for (size_t i = 0; i < n; ++i) a[i] -= b[i]; }
+static void vadd(double *a, const double *b, size_t n) {
+#pragma omp parallel for if (n >= PAR_MIN)
+    for (size_t i = 0; i < n; ++i) a[i] += b[i];
+}
+static void vsub(double *a, const double *b, size_t n) {
+#pragma omp parallel for if (n >= PAR_MIN)
+    for (size_t i = 0; i < n; ++i) a[i] -= b[i];
+}
 
 /* solve_douglas, FiniteDifferenceEngine.pyx:945-1006 */
 static void run_douglas(const engine_t *E, int n, double dt, double theta, double *V) {
@@ -557,6 +584,7 @@ static void run_hv(const engine_t *E, int n, double dt, double theta, double *V)
             F[k]->has_R = 0;
             op_apply(F[k], Y, E->n0, E->n1, T);
             F[k]->has_R = keep;
+#pragma omp parallel for if (N >= PAR_MIN)
             for (size_t i = 0; i < N; ++i) V[i] -= 0.5 * T[i];
         }
         for (int d = 0; d < nd; ++d) {
