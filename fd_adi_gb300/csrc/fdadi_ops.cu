@@ -9,7 +9,7 @@
 #include <stdarg.h>
 #include <string.h>
 
-#include <mutex>
+
 
 #include "fdadi_internal.cuh"
 
@@ -472,22 +472,15 @@ namespace fdadi {
 // FDADI_NOALLOC_MAX_ROWS doubles (8 MiB) per device.
 static __device__ __align__(256) double g_noalloc_scratch[FDADI_NOALLOC_MAX_ROWS];
 
-static std::mutex g_noalloc_mu;
-static double *g_noalloc_addr[64] = {nullptr};
-
-// Device address of g_noalloc_scratch on the current device, looked up once
-// per device (host code cannot use the symbol itself as a pointer).
+// Device address of g_noalloc_scratch on the current device (host code cannot
+// use the symbol itself as a pointer). It is looked up on every call rather
+// than cached: after cudaDeviceReset the module is loaded again and the array
+// may sit at a new address, so a cached pointer could go stale. Once the
+// module is loaded on the device the lookup does not synchronize or allocate.
 static int noalloc_scratch(double **out) {
-    int dev = 0;
-    FDADI_CUDA(cudaGetDevice(&dev));
-    FDADI_REQUIRE(dev >= 0 && dev < 64, "device ordinal %d out of range", dev);
-    std::lock_guard<std::mutex> g(g_noalloc_mu);
-    if (!g_noalloc_addr[dev]) {
-        void *p = nullptr;
-        FDADI_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-        g_noalloc_addr[dev] = static_cast<double *>(p);
-    }
-    *out = g_noalloc_addr[dev];
+    void *p = nullptr;
+    FDADI_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    *out = static_cast<double *>(p);
     return FDADI_OK;
 }
 

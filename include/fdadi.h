@@ -59,6 +59,26 @@ int fdadi_version(void);
 int fdadi_last_error(char *buf, size_t len);
 
 /* ------------------------------------------------------------------------ */
+/* Host-side meshes (no device work).                                       */
+/* ------------------------------------------------------------------------ */
+
+/* utils.exponential_space (FiniteDifference/utils.py:161-190) on the host:
+ * out[i] = l + (i*dv)**ex on [low, ~high], the upper end stretched so that
+ * `exact` lands on a point when force_exact is nonzero. Same operations and
+ * order as the reference's Python floats (C pow(), no contraction), so the
+ * mesh is bit-identical. FDADI_E_ARG with the reference's message "Did not
+ * find suitable value." when no point lies below `exact`. */
+int fdadi_exponential_space(double low, double exact, double high, double ex, int32_t size,
+                            int32_t force_exact, double *out);
+
+/* The variance meshes of n Heston engines, as HestonFiniteDifferenceEngine
+ * builds them (FiniteDifference/heston.py:384-389: exponential_space(0, v0[k],
+ * var_max, varexp, nv[k])), concatenated in option order into out
+ * (sum(nv) doubles), spread over `threads` host threads (0: all cores). */
+int fdadi_heston_var_meshes(int32_t n, const double *v0, const int32_t *nv, double var_max,
+                            double varexp, int32_t force_exact, int32_t threads, double *out);
+
+/* ------------------------------------------------------------------------ */
 /* Tridiagonal operator: replaces the C++ class _TriBandedOperator          */
 /* (FiniteDifference/_TriBandedOperatorGPU.cuh:21-85) behind                */
 /* BandedOperatorGPU.BandedOperator (FiniteDifference/BandedOperatorGPU.pxd).*/
@@ -99,9 +119,11 @@ int fdadi_tri_solve(const fdadi_tri_t *op, double *x, int64_t n0, int64_t n1,
  * device). No counterpart in the reference. The scratch is the library's own
  * static device array of FDADI_NOALLOC_MAX_ROWS doubles (8 MiB), held by
  * every device that loads the library until the process exits; operators with
- * more rows are rejected (FDADI_E_ARG). The first call on a device looks up
- * the array's device address (cudaGetSymbolAddress) and caches it; make that
- * first call before any stream capture. All calls share the array, so calls
+ * more rows are rejected (FDADI_E_ARG). Every call looks up the array's
+ * device address on the current device (cudaGetSymbolAddress), so the call
+ * stays valid after cudaDeviceReset; the first call on a device also loads the
+ * library's module there, so make it before any stream capture. All calls
+ * share the array, so calls
  * whose kernels overlap on the GPU race: order them. */
 #define FDADI_NOALLOC_MAX_ROWS (1 << 20)
 int fdadi_tri_solve_noalloc(const fdadi_tri_t *op, double *x, int64_t n0, int64_t n1,
@@ -287,12 +309,13 @@ int fdadi_heston_greeks(const fdadi_heston_batch_t *batch, void *workspace,
 /* The plan fdadi_heston_run uses for this batch when batch->plan is NULL. */
 int fdadi_heston_default_plan(const fdadi_heston_batch_t *batch, fdadi_heston_plan_t *plan);
 
-/* FP64 throughput probe: a dependent-chain-free DFMA loop on every SM;
- * writes one value per thread to out (>= blocks*threads doubles) and returns
- * the number of floating-point operations it issues (2 per DFMA) in *flops.
- * Used by the benchmark to measure the FP64 roofline on the device. */
+/* FP64 throughput probe: every thread runs `chains` (1, 2, 4, 8 or 16)
+ * independent DFMA chains for `iters` iterations; writes one value per thread
+ * to out (>= blocks*threads doubles) and returns the number of floating-point
+ * operations it issues (2 per DFMA) in *flops. Used by the benchmark to
+ * measure the FP64 roofline on the device. No reference counterpart. */
 int fdadi_fp64_probe(double *out, int32_t blocks, int32_t threads, int32_t iters,
-                     double *flops, void *stream);
+                     int32_t chains, double *flops, void *stream);
 
 /* ------------------------------------------------------------------------ */
 /* Pricing surrogate: BF16 tensor-core MLP kernels (no reference            */

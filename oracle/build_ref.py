@@ -1,7 +1,8 @@
 """Compat-build of the reference CPU ADI engine (test infrastructure only).
 
 This script is part of the checker, not of the product. It reads the
-reference's Cython/Python sources where they lie (``/root/reference``), makes
+reference's Cython/Python sources where they lie (``--reference DIR``, else the
+``FDADI_REFERENCE`` environment variable, else ``/root/reference``), makes
 build-time copies under ``oracle/_ref/FiniteDifference/`` (git-ignored), applies
 the minimal Python-3 compatibility edits listed below, cythonizes them with
 ``language_level=2`` and compiles them in place. Nothing it produces is
@@ -25,13 +26,16 @@ Compat edits (all made on the copies, never on the reference tree):
 * ``visualize.py`` is replaced by a stub whose ``fp`` is a no-op (the original
   uses Python 2 tuple parameters, visualize.py:186).
 
-Usage: ``python oracle/build_ref.py`` (needs Cython, run in a container where
-the reference tree exists). Exits 0 and prints ``skipped`` if it does not.
+Usage: ``python oracle/build_ref.py [--reference DIR]`` (needs Cython, run in a
+container where the reference tree exists). Exits 0 and prints ``skipped`` if it
+does not.
 
 ``python oracle/build_ref.py --from-generated`` compiles the C/C++ files that
 an earlier run generated (already under ``oracle/_ref/``) with this machine's
 compiler, Python and numpy headers, without Cython or the reference tree: the
 GPU host uses this to run the reference engine as the CPU baseline.
+``--auto`` does the first where the reference tree exists and the second
+otherwise.
 """
 import os
 import re
@@ -39,7 +43,7 @@ import shutil
 import subprocess
 import sys
 
-REF = "/root/reference/FiniteDifference"
+DEFAULT_REFERENCE = "/root/reference"
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
 PKG = os.path.join(OUT, "FiniteDifference")
@@ -104,7 +108,7 @@ def build_generated():
     procs = []
     for mod, src in srcs.items():
         cc = "g++" if src.endswith(".cpp") else "gcc"
-        cmd = [cc, "-O2", "-w", "-shared", "-fPIC"] + ["-I" + i for i in inc] + \
+        cmd = [cc, "-O2", "-w", "-shared", "-fPIC", "-ffp-contract=off"] + ["-I" + i for i in inc] + \
               [os.path.join(PKG, src), "-o", os.path.join(PKG, mod + suffix)]
         procs.append(subprocess.Popen(cmd))
     rc = max(p.wait() for p in procs)
@@ -114,8 +118,22 @@ def build_generated():
     return 0
 
 
-def main():
-    if "--from-generated" in sys.argv:
+def reference_tree(argv):
+    """The reference's FiniteDifference/ directory: --reference DIR, else
+    $FDADI_REFERENCE, else the default location."""
+    root = os.environ.get("FDADI_REFERENCE") or DEFAULT_REFERENCE
+    if "--reference" in argv:
+        i = argv.index("--reference")
+        if i + 1 >= len(argv):
+            raise SystemExit("--reference needs a directory")
+        root = argv[i + 1]
+    return os.path.join(root, "FiniteDifference")
+
+
+def main(argv=None):
+    argv = sys.argv[1:] if argv is None else argv
+    REF = reference_tree(argv)
+    if "--from-generated" in argv or ("--auto" in argv and not os.path.isdir(REF)):
         return build_generated()
     if not os.path.isdir(REF):
         print("build_ref: reference tree absent, skipped")
