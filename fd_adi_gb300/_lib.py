@@ -99,6 +99,12 @@ class Gemm(ctypes.Structure):
 SIGNATURES = {
     "fdadi_version": (ctypes.c_int, []),
     "fdadi_last_error": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t]),
+    "fdadi_exponential_space": (ctypes.c_int, [ctypes.c_double, ctypes.c_double,
+                                               ctypes.c_double, ctypes.c_double, ctypes.c_int32,
+                                               ctypes.c_int32, ctypes.c_void_p]),
+    "fdadi_heston_var_meshes": (ctypes.c_int, [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+                                               ctypes.c_double, ctypes.c_double, ctypes.c_int32,
+                                               ctypes.c_int32, ctypes.c_void_p]),
     "fdadi_tri_apply": (ctypes.c_int, [ctypes.POINTER(Tri), ctypes.c_void_p, ctypes.c_void_p,
                                        ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p]),
     "fdadi_tri_solve": (ctypes.c_int, [ctypes.POINTER(Tri), ctypes.c_void_p, ctypes.c_int64,
@@ -175,8 +181,8 @@ SIGNATURES = {
                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                          ctypes.c_void_p, ctypes.c_void_p]),
     "fdadi_fp64_probe": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
-                                        ctypes.c_int32, ctypes.POINTER(ctypes.c_double),
-                                        ctypes.c_void_p]),
+                                        ctypes.c_int32, ctypes.c_int32,
+                                        ctypes.POINTER(ctypes.c_double), ctypes.c_void_p]),
 }
 
 STAGE = {"explicit_douglas": 0, "explicit_hv0": 1, "explicit_hv3": 2, "explicit_implicit": 3,

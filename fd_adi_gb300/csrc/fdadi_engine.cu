@@ -1247,19 +1247,20 @@ __global__ void greeks_kernel(Arena A, const double *spots, const double *V, con
 }
 
 // Eight independent DFMA chains per thread: measures the FP64 pipe, not latency.
+template <int CHAINS>
 __global__ void fp64_probe_kernel(double *out, int iters) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    double a[8];
+    double a[CHAINS];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) a[k] = 1.0 + 1e-3 * (t + k);
+    for (int k = 0; k < CHAINS; ++k) a[k] = 1.0 + 1e-3 * (t + k);
     const double b = 0.999999999, c = 1e-9;
     for (int i = 0; i < iters; ++i) {
 #pragma unroll
-        for (int k = 0; k < 8; ++k) a[k] = fma(a[k], b, c);
+        for (int k = 0; k < CHAINS; ++k) a[k] = fma(a[k], b, c);
     }
     double s = 0.0;
 #pragma unroll
-    for (int k = 0; k < 8; ++k) s += a[k];
+    for (int k = 0; k < CHAINS; ++k) s += a[k];
     out[t] = s;
 }
 
@@ -2099,13 +2100,21 @@ int fdadi_heston_tune(const fdadi_heston_batch_t *b, void *workspace, int64_t ws
     return FDADI_OK;
 }
 
-int fdadi_fp64_probe(double *out, int32_t blocks, int32_t threads, int32_t iters, double *flops,
-                     void *stream) {
+int fdadi_fp64_probe(double *out, int32_t blocks, int32_t threads, int32_t iters,
+                     int32_t chains, double *flops, void *stream) {
     FDADI_REQUIRE(out && blocks > 0 && threads > 0 && threads <= 1024 && iters > 0,
                   "bad probe arguments");
-    fp64_probe_kernel<<<blocks, threads, 0, as_stream(stream)>>>(out, iters);
+    cudaStream_t st = as_stream(stream);
+    switch (chains) {
+    case 1: fp64_probe_kernel<1><<<blocks, threads, 0, st>>>(out, iters); break;
+    case 2: fp64_probe_kernel<2><<<blocks, threads, 0, st>>>(out, iters); break;
+    case 4: fp64_probe_kernel<4><<<blocks, threads, 0, st>>>(out, iters); break;
+    case 8: fp64_probe_kernel<8><<<blocks, threads, 0, st>>>(out, iters); break;
+    case 16: fp64_probe_kernel<16><<<blocks, threads, 0, st>>>(out, iters); break;
+    default: FDADI_REQUIRE(false, "probe chains must be 1, 2, 4, 8 or 16 (got %d)", (int)chains);
+    }
     FDADI_CHECK_LAUNCH();
-    if (flops) *flops = 2.0 * 8.0 * (double)blocks * threads * (double)iters;
+    if (flops) *flops = 2.0 * (double)chains * (double)blocks * threads * (double)iters;
     return FDADI_OK;
 }
 
