@@ -203,6 +203,89 @@ class HestonBatch(object):
     def _sptr(self):
         return ctypes.c_void_p(self.stream.cuda_stream)
 
+    def price_calls(self, spot, strikes, variance, params, dt, V=None, put=False,
+                    spot_max_factor=8.0, var_max=5.0, spotdensity=7.0, varexp=4.0,
+                    threads=0):
+        """Price a new set of options on this batch's grid sizes, from their
+        parameters (host arrays in, host prices out), as the reference engine
+        does per option (FiniteDifferenceEngineGPU.pyx:662-686 builds the
+        meshes, heston.py:402 the payoff, :461-469 reads the price).
+
+        Host: every option's meshes (spot: sinh mesh on [0, ~spot_max_factor
+        K] clustered at K; variance: exponential mesh on [0, ~var_max]; the
+        grid point nearest the spot moved onto it), bit-identical to
+        mesh.heston_meshes, and each price's arena index. Device: the meshes,
+        parameters, steps and strikes copied from pinned memory on the batch's
+        stream, the operators and factors rebuilt, the payoff, the time loop
+        and the price gather; the prices come back to pinned memory.
+
+        spot, variance: scalars or [n]; strikes, dt: [n]; params: [n, 5] of
+        (r, kappa, theta, sigma, rho). V: the device state arena to use
+        (allocated on first use). Returns a numpy array of n prices (a view
+        of this batch's pinned buffer: copy it to keep it past the next call)."""
+        n = self.n
+        strikes = np.ascontiguousarray(strikes, dtype=np.float64).reshape(-1)
+        params = np.ascontiguousarray(params, dtype=np.float64).reshape(n, 5)
+        dt = np.broadcast_to(np.asarray(dt, dtype=np.float64), (n,))
+        if strikes.size != n:
+            raise ValueError("need %d strikes, got %d" % (n, strikes.size))
+        spot = np.broadcast_to(np.asarray(spot, dtype=np.float64), (n,))
+        variance = np.broadcast_to(np.asarray(variance, dtype=np.float64), (n,))
+        spots, vars_ = _mesh.heston_meshes_batch(spot, strikes, variance, self.n0, self.n1,
+                                                 spot_max_factor * strikes, var_max,
+                                                 spotdensity, varexp, threads=threads)
+        flat = self.p_off[:-1] + _mesh.price_index_batch(spots, vars_, self.n0, self.n1, spot,
+                                                         variance)
+        if not hasattr(self, "_h"):
+            pin = lambda t: t.pin_memory()
+            self._h = dict(spots=pin(torch.empty(self.spots.numel(), dtype=torch.float64)),
+                           vars=pin(torch.empty(self.vars.numel(), dtype=torch.float64)),
+                           params=pin(torch.empty(n * 5, dtype=torch.float64)),
+                           dt=pin(torch.empty(n, dtype=torch.float64)),
+                           K=pin(torch.empty(n, dtype=torch.float64)),
+                           idx=pin(torch.empty(n, dtype=torch.int64)),
+                           prices=pin(torch.empty(n, dtype=torch.float64)))
+            self._d = dict(K=torch.empty(n, dtype=torch.float64, device=self.device),
+                           idx=torch.empty(n, dtype=torch.int64, device=self.device),
+                           prices=torch.empty(n, dtype=torch.float64, device=self.device))
+        h, d = self._h, self._d
+        # the previous call's copies have completed (it synchronized)
+        h["spots"].numpy()[:] = spots
+        h["vars"].numpy()[:] = vars_
+        h["params"].numpy()[:] = params.reshape(-1)
+        h["dt"].numpy()[:] = dt
+        h["K"].numpy()[:] = strikes
+        h["idx"].numpy()[:] = flat
+        if V is None:
+            if getattr(self, "_V", None) is None:
+                self._V = torch.empty(self.total_points, dtype=torch.float64, device=self.device)
+            V = self._V
+        self._check_state(V)
+        with torch.cuda.stream(self.stream):
+            self.stream.wait_stream(torch.cuda.current_stream(self.device))
+            self.spots.copy_(h["spots"], non_blocking=True)
+            self.vars.copy_(h["vars"], non_blocking=True)
+            self.params.view(-1).copy_(h["params"], non_blocking=True)
+            self.dt.copy_(h["dt"], non_blocking=True)
+            d["K"].copy_(h["K"], non_blocking=True)
+            d["idx"].copy_(h["idx"], non_blocking=True)
+            self._prepare()
+            self.payoff(d["K"], V, put=put)
+            self.run(V)
+            self.gather(V, d["idx"], d["prices"])
+            h["prices"].copy_(d["prices"], non_blocking=True)
+        self.stream.synchronize()
+        return h["prices"].numpy()
+
+    def price_calls_last(self):
+        """The prices of the last price_calls() (a copy)."""
+        return self._h["prices"].numpy().copy()
+
+    @property
+    def price_calls_h2d_bytes(self):
+        """Host-to-device bytes one price_calls() copies."""
+        return 8 * (int(self.spots.numel()) + int(self.vars.numel()) + 5 * self.n + 4 * self.n)
+
     def _prepare(self):
         with torch.cuda.stream(self.stream):
             _lib.call("fdadi_heston_prepare", ctypes.byref(self.struct),

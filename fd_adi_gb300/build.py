@@ -12,10 +12,21 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libfdadi.so")
-SOURCES = ["fdadi_ops.cu", "fdadi_engine.cu", "fdadi_mlp.cu"]
+SOURCES = ["fdadi_ops.cu", "fdadi_engine.cu", "fdadi_mlp.cu", "fdadi_mesh.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
               "-I" + os.path.join(ROOT, "include")]
+# Host-only sources restate the reference's Python float arithmetic: no
+# floating-point contraction (a fused multiply-add would change the bits).
+CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-pthread",
+             "-I" + os.path.join(ROOT, "include")]
+
+
+def _cuda_include():
+    for d in (os.environ.get("CUDA_HOME"), "/usr/local/cuda"):
+        if d and os.path.isdir(os.path.join(d, "include")):
+            return os.path.join(d, "include")
+    return None
 
 
 def _nvcc():
@@ -50,7 +61,12 @@ def build(force=False, verbose=False):
 
     def compile_one(src):
         obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
-        cmd = [nvcc] + ARCH + NVCC_FLAGS + ["-c", os.path.join(CSRC, src), "-o", obj]
+        if src.endswith(".cpp"):
+            inc = _cuda_include()
+            cmd = [os.environ.get("CXX", "g++")] + CXX_FLAGS + \
+                (["-I" + inc] if inc else []) + ["-c", os.path.join(CSRC, src), "-o", obj]
+        else:
+            cmd = [nvcc] + ARCH + NVCC_FLAGS + ["-c", os.path.join(CSRC, src), "-o", obj]
         if verbose:
             print(" ".join(cmd))
         subprocess.check_call(cmd)
@@ -59,7 +75,7 @@ def build(force=False, verbose=False):
     with concurrent.futures.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
     tmp = LIB + ".%d.tmp" % os.getpid()
-    subprocess.check_call([nvcc] + ARCH + ["-shared", "-o", tmp] + objs)
+    subprocess.check_call([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread"])
     os.replace(tmp, LIB)
     return LIB
 
