@@ -44,9 +44,24 @@ HV_THETA = 0.5 + np.sqrt(3.0) / 6.0
 # 8 -> 256 x 4 -> 2 (the padding to 16 inputs and 128/16 outputs is not counted).
 NET_FLOPS = 2.0 * (8 * 256 + 3 * 256 * 256 + 256 * 2)
 
-STAGE_BYTES = {"explicit_hv0": 32, "explicit_hv3": 40, "spot_solve": 24, "var_solve_y2": 16,
-               "var_solve_v": 16, "explicit_implicit": 16, "var_solve_implicit": 16,
-               "spot_solve_implicit": 16}
+# Algorithmic state bytes per grid point of each stage: the per-stage figures
+# of the unit "one grid point x one time step" (FP64 state grids only; operator
+# coefficients and Thomas factors are counted as cached). HV step = 144 B:
+# Y0 16 (read V, write Y0) + Y1 24 + Y2 24 + corrector 32 (read Y0, Y2, V;
+# write) + two corrector solves 24 each. Implicit step = 40 B: the mixed
+# explicit part 16 + two solves 12 each. The fused kernels read and write more
+# or less than these (KERNEL_IO_BYTES), but the roofline counts these.
+STAGE_BYTES = {"explicit_hv0": 16, "explicit_hv3": 32, "spot_solve": 24, "var_solve_y2": 24,
+               "var_solve_v": 24, "explicit_implicit": 16, "var_solve_implicit": 12,
+               "spot_solve_implicit": 12}
+HV_STEP_BYTES = 144
+HV_STEP_STAGES = ["explicit_hv0", "spot_solve", "var_solve_y2", "explicit_hv3", "spot_solve",
+                  "var_solve_v"]
+# The state bytes each fused kernel itself reads and writes per point (its own
+# input and output grids): the predictor reads V and writes F(V), W and F1 V.
+KERNEL_IO_BYTES = {"explicit_hv0": 32, "explicit_hv3": 40, "spot_solve": 24, "var_solve_y2": 16,
+                   "var_solve_v": 16, "explicit_implicit": 16, "var_solve_implicit": 16,
+                   "spot_solve_implicit": 16}
 # DRAM bytes per grid point per launch measured by ncu (--set full) on the
 # 256-option cut of the batch workload (profiles/explicit_hv_batch256.md and
 # profiles/line_solves_batch256.md); its state, operators and Thomas factors
@@ -201,25 +216,49 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def fp64_peak(torch):
-    """FP64 FMA throughput of this device, measured with the library's probe."""
+def fp64_peak(torch, index=0, seconds=1.2):
+    """FP64 FMA throughput of this device, measured with the library's probe:
+    a full-occupancy DFMA loop (8 blocks of 256 threads per SM) with 1, 2, 4, 8
+    and 16 independent chains per thread, each run for about `seconds` while
+    nvidia-smi samples the SM clock. Returns the best rate (TFLOP/s) and the
+    sweep: per chain count its rate, the median SM clock during it and the
+    DFMA thread-instructions it retired per SM per clock cycle."""
     from fd_adi_gb300 import _lib
     dev = torch.cuda.current_device()
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
-    blocks, threads, iters = sms * 8, 256, 4096
+    blocks, threads = sms * 8, 256
     out = torch.empty(blocks * threads, dtype=torch.float64, device="cuda")
     flops = ctypes.c_double()
     st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
-    best = 0.0
-    for _ in range(4):
+
+    def run(chains, iters):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
         _lib.call("fdadi_fp64_probe", ctypes.c_void_p(out.data_ptr()), blocks, threads, iters,
-                  ctypes.byref(flops), st)
+                  chains, ctypes.byref(flops), st)
         e1.record()
         e1.synchronize()
-        best = max(best, flops.value / (e0.elapsed_time(e1) * 1e-3))
-    return best / 1e12
+        return flops.value, e0.elapsed_time(e1) * 1e-3
+
+    sweep = {}
+    best = 0.0
+    for chains in (1, 2, 4, 8, 16):
+        f, t = run(chains, 256)
+        iters = max(256, int(256 * seconds / max(t, 1e-6)))
+        iters = min(iters, 1 << 30)
+        clk = Clocks(index)
+        clk.start()
+        time.sleep(0.25)
+        f, t = run(chains, iters)
+        c = clk.stop()
+        rate = f / t
+        mhz = c.get("sm_mhz")
+        per_clk = (f / 2.0 / t / sms / (mhz * 1e6)) if mhz else None
+        sweep[str(chains)] = {"tflops": round(rate / 1e12, 4), "seconds": round(t, 3),
+                              "sm_mhz": mhz, "dfma_per_sm_per_clk": (round(per_clk, 3)
+                                                                     if per_clk else None)}
+        best = max(best, rate)
+    return best / 1e12, sweep
 
 
 def stage_times(batch, V, torch):
@@ -308,11 +347,47 @@ def plain_vs_batched(torch, n_batch=2048):
     torch.cuda.synchronize()
     batched = reps * n_batch / (e0.elapsed_time(e1) * 1e-3)
     p_batch = float(out[0].item())
+    # the fused engine on one option at a time: one CUDA graph per option
+    # (the same kernels as the batch, a batch of 1), timed on the device
+    b1 = HestonBatch([opt], [(S, v)], scheme="douglas", n_steps=n - 1, dt=dt, theta=0.5,
+                     implicit_steps=2, implicit_dt_factor=0.5, graph=True, plan="auto")
+    V10 = b1.pack([grid_host])
+    V1 = torch.empty_like(V10)
+    idx1 = b1.flat_index()
+    out1 = torch.empty(1, dtype=torch.float64, device="cuda")
+
+    def single_once():
+        with torch.cuda.stream(b1.stream):
+            b1._prepare()
+            V1.copy_(V10, non_blocking=True)
+            b1.run(V1)
+            b1.gather(V1, idx1, out1)
+
+    for _ in range(3):
+        single_once()
+    torch.cuda.synchronize()
+    reps1 = 20
+    e0.record(b1.stream)
+    for _ in range(reps1):
+        single_once()
+    e1.record(b1.stream)
+    torch.cuda.synchronize()
+    single = reps1 / (e0.elapsed_time(e1) * 1e-3)
+    p_single = float(out1[0].item())
     return {"config": "150x150, nt=150, 2 implicit half-steps + Douglas theta=0.5",
             "plain_options_per_s": plain, "batched_options_per_s": batched,
             "ratio": batched / plain, "batch": n_batch, "plan": b.plan,
-            "price_plain": p_plain, "price_batched": p_batch,
-            "price_rel_diff": abs(p_plain - p_batch) / abs(p_plain)}
+            "plain_note": "per-operator engine: the reference's per-step call sequence, about "
+                          "a dozen small launches per step issued from Python through ctypes; "
+                          "its time is mostly host launch overhead, not GPU work",
+            "fused_single_options_per_s": single,
+            "ratio_vs_fused_single": batched / single,
+            "fused_single_note": "fused engine with a batch of 1 option: the operator build, "
+                                 "then the time loop (%d launches) replayed from one CUDA "
+                                 "graph per option (device-timed)" % b1.launches_per_run,
+            "price_plain": p_plain, "price_batched": p_batch, "price_fused_single": p_single,
+            "price_rel_diff": abs(p_plain - p_batch) / abs(p_plain),
+            "price_rel_diff_single": abs(p_single - p_batch) / abs(p_batch)}
 
 
 def run_gemm(args):
@@ -493,14 +568,15 @@ def run_surrogate(args):
     return 0
 
 
-def cpu_baseline(w, n_sample, nt_sample=None):
+def cpu_baseline(w, n_sample, nt_sample=None, want_results=False):
     """The reference CPU engine (compiled from its generated sources on this
     host, kind "reference") or, where it does not import, the C restatement
     of it (kind "port"), on all host cores (one single-threaded process per
     core, options spread over them), on n_sample options spread through the
     workload and, when nt_sample is given, only that many time steps of each.
     The sample's grid-point-step rate is converted to options of the
-    workload's mean grid size."""
+    workload's mean grid size. With want_results, also returns the sample's
+    option indices, prices and final grids (for the parity check)."""
     n = len(w["K"])
     idx = sorted(set(np.linspace(0, n - 1, n_sample).astype(int).tolist()))
     nt = w["nt"]
@@ -513,8 +589,8 @@ def cpu_baseline(w, n_sample, nt_sample=None):
         for var in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
             os.environ[var] = "1"
         jobs = [(w["S0"], w["K"][k], w["r"][k], w["kappa"][k], w["theta"][k], w["sigma"][k],
-                 w["rho"][k], w["v0"][k], w["T"][k] * nrun / nt, w["nS"][k], w["nv"][k], nrun)
-                for k in idx]
+                 w["rho"][k], w["v0"][k], w["T"][k] * nrun / nt, w["nS"][k], w["nv"][k], nrun,
+                 want_results) for k in idx]
         with mp.get_context("spawn").Pool(min(cores, len(jobs))) as pool:
             pool.map(H.price_option, jobs[:1])       # warm the workers' imports
             t0 = time.perf_counter()
@@ -522,6 +598,8 @@ def cpu_baseline(w, n_sample, nt_sample=None):
             dt = time.perf_counter() - t0
         kind = "reference"
         what = "reference CPU engine (FiniteDifferenceEngine.pyx, compat build)"
+        prices = [x[0] for x in res]
+        grids = [x[3] for x in res]
     else:
         from oracle import oracle as O
         meshes = meshes_for(w, idx)
@@ -530,34 +608,64 @@ def cpu_baseline(w, n_sample, nt_sample=None):
                    ("hv", nrun - 1, w["T"][k] / nt, HV_THETA)] for k in idx]
         O.build()
         t0 = time.perf_counter()
-        O.heston_batch(meshes, params_of(w, idx), V0, scheds, nthreads=cores)
+        grids = O.heston_batch(meshes, params_of(w, idx), V0, scheds, nthreads=cores)
         dt = time.perf_counter() - t0
         kind = "port"
         what = "C restatement of the reference engine (oracle)"
+        from fd_adi_gb300 import mesh as M
+        prices = [float(g[M.price_index(m[0], m[1], w["S0"], w["v0"][k])])
+                  for g, m, k in zip(grids, meshes, idx)]
     pts = float(sum(int(w["nS"][k]) * int(w["nv"][k]) for k in idx)) * nrun
-    return {"value": pts / dt / mean_pts, "unit": UNIT, "cores": min(cores, len(idx)),
-            "kind": kind,
-            "sample": "%s: %d options spread through the %d-option workload, %d of %d time "
-                      "steps (%.3g grid-point-steps) on %d cores in %.1f s = %.3g "
-                      "grid-point-steps/s, scaled to the workload's mean option"
-                      % (what, len(idx), n, nrun, nt, pts, min(cores, len(idx)), dt, pts / dt)}
+    out = {"value": pts / dt / mean_pts, "unit": UNIT, "cores": min(cores, len(idx)),
+           "kind": kind, "elapsed_s": dt,
+           "sample": "%s: %d options spread through the %d-option workload, %d of %d time "
+                     "steps (%.3g grid-point-steps) on %d cores in %.1f s = %.3g "
+                     "grid-point-steps/s, scaled to the workload's mean option"
+                     % (what, len(idx), n, nrun, nt, pts, min(cores, len(idx)), dt, pts / dt)}
+    if want_results:
+        return out, (idx, prices, grids)
+    return out
+
+
+def parity(batch, V, prices, sample):
+    """The GPU's prices and final grids against the CPU engine's on the same
+    options: max relative price difference, and max grid difference relative
+    to each grid's max-norm (bars: 1e-10 and 1e-9)."""
+    idx, ref_prices, ref_grids = sample
+    got = prices.cpu().numpy()
+    Vh = V.cpu().numpy()
+    prel, grel = [], []
+    for k, p, g in zip(idx, ref_prices, ref_grids):
+        prel.append(abs(got[k] - p) / max(abs(p), 1e-300))
+        if g is not None:
+            mine = Vh[batch.p_off[k]:batch.p_off[k + 1]].reshape(batch.n0[k], batch.n1[k])
+            grel.append(float(np.abs(mine - g).max() / max(np.abs(g).max(), 1e-300)))
+    return {"n": len(idx), "max_price_rel": float(max(prel)),
+            "max_grid_rel_on_sample": float(max(grel)) if grel else None,
+            "price_bar": 1e-10, "grid_bar": 1e-9,
+            "ok": bool(max(prel) <= 1e-10 and (not grel or max(grel) <= 1e-9))}
 
 
 def run_reference(args, rank, world):
     if rank != 0:
         return 0
     w = workload_large() if args.workload == "large" else workload(args.options, args.seed)
-    rates = []
+    rates, elapsed = [], []
     for s in range(args.warmup + args.steps):
         cb = cpu_baseline(w, args.ref_sample, 20 if args.workload == "large" else None)
         if s >= args.warmup:
             rates.append(cb["value"])
+            elapsed.append(cb["elapsed_s"])
     value = float(np.mean(rates))
     cb["value"] = value
-    times = [len(w["K"]) / r for r in rates]
+    # a step is the bounded sample (its wall time is measured); the whole
+    # workload's time at this rate is reported beside it
+    sample_ms = [x * 1e3 for x in elapsed]
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": float(np.mean(times)) * 1e3, "higher_is_better": True,
+            "ms_per_step": float(np.mean(sample_ms)),
+            "ms_per_workload_extrapolated": len(w["K"]) / value * 1e3,
+            "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "impl": "reference",
             "config": config_block(args, w),
@@ -653,24 +761,28 @@ def main():
                         plan=(json.loads(args.plan) if args.plan else
                               None if args.no_tune else "auto"))
     t_tune = time.perf_counter() - t_tune
-    # device-resident inputs (value) and pinned host copies (e2e)
+    # device-resident inputs (value); e2e prices from the options' parameters
     V0_dev = batch.pack(payoffs(w, meshes))
     V = torch.empty_like(V0_dev)
-    h_spots = batch.spots.cpu().pin_memory()
-    h_vars = batch.vars.cpu().pin_memory()
-    h_params = batch.params.cpu().pin_memory()
-    h_dt = batch.dt.cpu().pin_memory()
     # the initial grids are the calls' payoffs, built on the device from the
     # strikes (checked once against the host-built grids)
     K_dev = torch.tensor(w["K"], dtype=torch.float64, device="cuda")
-    h_K = K_dev.cpu().pin_memory()
     batch._prepare()
     if not torch.equal(batch.payoff(K_dev, V), V0_dev):
         raise RuntimeError("device payoff differs from the host-built initial grids")
     flat_idx = batch.flat_index([(w["S0"], v0) for v0 in w["v0"]])
     prices = torch.empty(batch.n, dtype=torch.float64, device="cuda")
-    h_prices = torch.empty(batch.n, dtype=torch.float64).pin_memory()
     stream = batch.stream
+    # the batched host mesh generator (timed inside e2e) against the
+    # per-option generators (untimed, above), once
+    from fd_adi_gb300 import mesh as M
+    sb, vb = M.heston_meshes_batch(w["S0"], w["K"], w["v0"], w["nS"], w["nv"], 8.0 * w["K"], 5.0)
+    mesh_bitwise = bool(np.array_equal(sb, np.concatenate([m[0] for m in meshes])) and
+                        np.array_equal(vb, np.concatenate([m[1] for m in meshes])))
+    idx_b = batch.p_off[:-1] + M.price_index_batch(sb, vb, w["nS"], w["nv"], w["S0"], w["v0"])
+    mesh_bitwise = mesh_bitwise and bool(np.array_equal(idx_b, flat_idx.cpu().numpy()))
+    h_params = np.array(params, dtype=np.float64)
+    h_dt = np.asarray(dts, dtype=np.float64)
 
     def step_device():
         with torch.cuda.stream(stream):
@@ -680,17 +792,9 @@ def main():
             batch.gather(V, flat_idx, prices)
 
     def step_e2e():
-        with torch.cuda.stream(stream):
-            batch.spots.copy_(h_spots, non_blocking=True)
-            batch.vars.copy_(h_vars, non_blocking=True)
-            batch.params.copy_(h_params, non_blocking=True)
-            batch.dt.copy_(h_dt, non_blocking=True)
-            K_dev.copy_(h_K, non_blocking=True)
-            batch._prepare()
-            batch.payoff(K_dev, V)
-            batch.run(V)
-            batch.gather(V, flat_idx, prices)
-            h_prices.copy_(prices, non_blocking=True)
+        # parameters in, prices out: host meshes and price indices, copies
+        # from pinned memory, operators, payoff, time loop, gather, prices back
+        return batch.price_calls(w["S0"], w["K"], w["v0"], h_params, h_dt, V=V)
 
     def timed(fn, k):
         if world > 1:
@@ -724,14 +828,26 @@ def main():
     clocks_e2e = Clocks(local)
     clocks_e2e.start()
     time.sleep(0.3)
+    t_wall = time.perf_counter()
     ms_e2e = timed(step_e2e, max(1, args.steps))
+    t_wall = (time.perf_counter() - t_wall) * 1e3 / max(1, args.steps)
+    # the step's host work (meshes) leaves the stream idle between events, so
+    # the events already span it; the wall clock bounds it from above
+    ms_e2e = max(ms_e2e, t_wall) if world == 1 else ms_e2e
     clk_e2e = clocks_e2e.stop()
+    t_mesh = time.perf_counter()
+    M.heston_meshes_batch(w["S0"], w["K"], w["v0"], w["nS"], w["nv"], 8.0 * w["K"], 5.0)
+    t_mesh = (time.perf_counter() - t_mesh) * 1e3
+    # the last step's final grids and prices, kept for the parity check (the
+    # per-stage timing below advances V again)
+    V_final = V.clone()
+    prices_final = torch.as_tensor(batch.price_calls_last(), dtype=torch.float64)
 
     n_total = len(w_all["K"])
     value = n_total / (ms * 1e-3)
     e2e_value = n_total / (ms_e2e * 1e-3)
-    h2d = sum(t.numel() * t.element_size() for t in (h_spots, h_vars, h_params, h_dt, h_K))
-    d2h = h_prices.numel() * 8
+    h2d = batch.price_calls_h2d_bytes
+    d2h = batch.n * 8
     # per step: the run, 4 prepare kernels, the payoff and the price gather
     launches = args.steps * (batch.launches_per_run + 4 + 2)
 
@@ -743,31 +859,49 @@ def main():
         avg_ms = st[dom][0]
         hbm_peak, peak_src = measured_peaks()
         ach = STAGE_BYTES[dom] * P / (avg_ms * 1e-3) / 1e9
-        fp64 = fp64_peak(torch)
+        fp64, probe = fp64_peak(torch, local)
         fp_ach = STAGE_FLOPS[dom] * P / (avg_ms * 1e-3) / 1e12
         pts_steps = float(P) * nt
+        hv_step_ms = sum(st[k][0] for k in HV_STEP_STAGES if k in st)
+        hv_step_gbs = HV_STEP_BYTES * P / (hv_step_ms * 1e-3) / 1e9
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                "dtype": "f64", "data": "synthetic", "config": config_block(args, w),
                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                        "d2h_bytes_per_step": int(d2h), "ms_per_step": ms_e2e,
+                       "api": "HestonBatch.price_calls: option parameters in (host numpy), "
+                              "prices out (host); each step builds every option's meshes on "
+                              "the host (timed), copies meshes, parameters, steps and strikes "
+                              "from pinned memory, rebuilds the operators, runs and reads back",
+                       "host_mesh_ms": round(t_mesh, 2), "mesh_bitwise": mesh_bitwise,
                        "clocks": clk_e2e},
                "gpu_launches": int(launches),
                "grid_point_steps_per_s": pts_steps * world / (ms * 1e-3),
-               "roofline": {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": hbm_peak,
-                            "unit": "GB/s", "frac": ach / hbm_peak,
+               # the dominant kernel is bound by the FP64 pipe: its FP64 work per
+               # launch over its event-timed duration, against the live DFMA probe
+               "roofline": {"bound": "fp64", "kernel": dom, "achieved": fp_ach, "peak": fp64,
+                            "unit": "TFLOP/s", "frac": fp_ach / fp64,
+                            "flops_per_point": STAGE_FLOPS[dom],
+                            "flops_note": "2 x FP64 instructions per grid point (a DMUL or "
+                                          "DADD holds the FP64 pipe like a DFMA)",
+                            "peak_source": "measured live: fdadi_fp64_probe, best of 1-16 "
+                                           "DFMA chains per thread, ~1.2 s each",
                             "traffic": (NCU_TRAFFIC_B_PER_POINT[dom] * P
                                         if dom in NCU_TRAFFIC_B_PER_POINT else None),
                             "traffic_source": "ncu dram__bytes_read+write per point (256-option "
                                               "capture) x points of this launch",
-                            "peak_source": peak_src,
-                            "bytes_per_point": STAGE_BYTES[dom],
-                            "avg_launch_ms": avg_ms, "launches": st[dom][1]},
-               "fp64_pipe": {"kernel": dom, "achieved": fp_ach, "peak": fp64,
-                             "unit": "TFLOP/s (2 x FP64 instructions/s)", "frac": fp_ach / fp64,
-                             "peak_source": "measured live (fdadi_fp64_probe, DFMA only)",
-                             "flops_per_point": STAGE_FLOPS[dom]},
+                            "avg_launch_ms": avg_ms, "launches": st[dom][1],
+                            "points_per_launch": int(P),
+                            # the same launch against HBM, by the algorithmic
+                            # state bytes of this stage
+                            "hbm": {"achieved": ach, "peak": hbm_peak, "unit": "GB/s",
+                                    "frac": ach / hbm_peak, "bytes_per_point": STAGE_BYTES[dom],
+                                    "peak_source": peak_src},
+                            # one whole HV step (six stage launches) at 144 B per point
+                            "hv_step": {"ms": hv_step_ms, "bytes_per_point": HV_STEP_BYTES,
+                                        "gbs": hv_step_gbs, "hbm_frac": hv_step_gbs / hbm_peak}},
+               "fp64_probe": probe,
                "stage_ms": {k: round(v[0], 4) for k, v in st.items()},
                # per stage: algorithmic GB/s (state bytes per point x points /
                # launch time) against the HBM copy peak, and the FP64 pipe's share
@@ -786,8 +920,12 @@ def main():
                             setup_s=round(t_tune, 2)),
                "clocks": clk}
         if args.cpu_sample > 0:
-            out["cpu_baseline"] = cpu_baseline(
-                w, args.cpu_sample, 20 if args.workload == "large" else None)
+            full = args.workload != "large"
+            cb = cpu_baseline(w, args.cpu_sample, None if full else 20, want_results=full)
+            if full:
+                cb, sample = cb
+                out["parity"] = parity(batch, V_final, prices_final, sample)
+            out["cpu_baseline"] = cb
         if not args.no_extras:
             out["plain_vs_batched"] = plain_vs_batched(torch)
     if world > 1:

@@ -121,12 +121,13 @@ def quiet(fn, *a, **k):
 
 def price_option(job):
     """Price one Heston call with the reference engine (for a process pool):
-    job = (S0, K, r, kappa, theta, sigma, rho, v0, T, nS, nv, nt); the mesh as
-    the reference builds it (S_max = 8K, v_max = 5), two implicit half-steps then
-    HV theta = 1/2 + sqrt(3)/6 for the remaining steps. Returns (price,
-    grid-point-steps, seconds of the time loop)."""
+    job = (S0, K, r, kappa, theta, sigma, rho, v0, T, nS, nv, nt[, want_grid]);
+    the mesh as the reference builds it (S_max = 8K, v_max = 5), two implicit
+    half-steps then HV theta = 1/2 + sqrt(3)/6 for the remaining steps. Returns
+    (price, grid-point-steps, seconds of the time loop, final grid or None)."""
     import time
-    S0, K, r, kappa, theta, sigma, rho, v0, T, nS, nv, nt = job
+    S0, K, r, kappa, theta, sigma, rho, v0, T, nS, nv, nt = job[:12]
+    want_grid = len(job) > 12 and bool(job[12])
     spots, vars_ = heston_mesh(S0, K, v0, int(nS), int(nv), 8.0 * K, 5.0)
     F = heston_engine(S0, K, r, v0, kappa, theta, sigma, rho, spots, vars_)
     V0 = F.grid.domain[-1].copy()
@@ -136,4 +137,5 @@ def price_option(job):
     V = quiet(F.solve_hundsdorferverwer, int(nt) - 1, dt, initial=V,
               theta=0.5 + np.sqrt(3.0) / 6.0)
     t = time.perf_counter() - t0
-    return float(V[price_index(spots, vars_, S0, v0)]), float(nS) * nv * nt, t
+    return (float(V[price_index(spots, vars_, S0, v0)]), float(nS) * nv * nt, t,
+            np.asarray(V) if want_grid else None)
