@@ -51,6 +51,7 @@ struct GemmArgs {
     int M, N, K;
     int act;          // 0: none, 1: SiLU, 2: multiply by SiLU'(aux)
     int *status;      // set to 1 if an mbarrier wait timed out
+    long long wait;   // wait limit in clock cycles (0: GM_WAIT_CYCLES); < 0: abort test
 };
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {
@@ -303,7 +304,8 @@ struct WsArgs {
 };
 
 // Bounded wait that gives up when another role has aborted.
-__device__ __forceinline__ bool ws_wait(uint64_t *mbar, uint32_t parity, volatile int *abort) {
+__device__ __forceinline__ bool ws_wait(uint64_t *mbar, uint32_t parity, volatile int *abort,
+                                        long long limit = GM_WAIT_CYCLES) {
     const long long t0 = clock64();
     uint32_t done = 0;
     while (!done) {
@@ -313,7 +315,7 @@ __device__ __forceinline__ bool ws_wait(uint64_t *mbar, uint32_t parity, volatil
             : "=r"(done) : "r"(smem_addr(mbar)), "r"(parity) : "memory");
         if (done) break;
         if (*abort) return false;
-        if (clock64() - t0 > GM_WAIT_CYCLES) {
+        if (clock64() - t0 > limit) {
             *abort = 1;
             return false;
         }
@@ -334,7 +336,8 @@ __device__ __forceinline__ bool mbar_test(uint64_t *mbar, uint32_t parity) {
 // ws_wait for barriers that complete slowly (a whole layer's MMAs or
 // epilogue): backs off with __nanosleep between polls so that waiting warps
 // leave the issue slots to the warps doing the work.
-__device__ __forceinline__ bool ws_wait_slow(uint64_t *mbar, uint32_t parity, volatile int *abort) {
+__device__ __forceinline__ bool ws_wait_slow(uint64_t *mbar, uint32_t parity, volatile int *abort,
+                                             long long limit = GM_WAIT_CYCLES) {
     const long long t0 = clock64();
     uint32_t done = 0;
     while (true) {
@@ -344,7 +347,7 @@ __device__ __forceinline__ bool ws_wait_slow(uint64_t *mbar, uint32_t parity, vo
             : "=r"(done) : "r"(smem_addr(mbar)), "r"(parity) : "memory");
         if (done) return true;
         if (*abort) return false;
-        if (clock64() - t0 > GM_WAIT_CYCLES) {
+        if (clock64() - t0 > limit) {
             *abort = 1;
             return false;
         }
@@ -387,6 +390,9 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
     const uint32_t ncols = 2 * N <= 32 ? 32 : 2 * N <= 64 ? 64 : 2 * N <= 128 ? 128
                          : 2 * N <= 256 ? 256 : 512;
     const int units = w.m_tiles * w.ksplit * w.problems;
+    // the limit of every wait of the main loop; the drains after an abort keep
+    // the default limit, so copies and MMAs in flight always land first
+    const long long lim = g.wait > 0 ? g.wait : GM_WAIT_CYCLES;
 
     if (tid == 0) {
         for (int s = 0; s < WS_STAGES; ++s) {
@@ -426,7 +432,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
                 for (int k0 = k_lo; k0 < k_hi; k0 += GM_BK, ++it) {
                     const int s = it % WS_STAGES;
                     const uint32_t n = it / WS_STAGES;
-                    if (n > 0 && !ws_wait(&empty[s], (n - 1) & 1, abort)) { ok = false; break; }
+                    if (n > 0 && !ws_wait(&empty[s], (n - 1) & 1, abort, lim)) { ok = false; break; }
                     const int kc = min(GM_BK, k_hi - k0) >> 3;
                     const uint32_t bytes = (uint32_t)kc * (GM_BM + N) * 16;
                     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
@@ -446,13 +452,17 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
             for (uint32_t j = last > WS_STAGES ? last - WS_STAGES : 0; j < last; ++j) {
                 const int s = j % WS_STAGES;
                 const uint32_t n = j / WS_STAGES;
-                if (*abort) mbar_wait(&full[s], n & 1);   // copies in flight
-                else ws_wait(&empty[s], n & 1, abort);
+                // after an abort (or if this wait gives up), wait only for
+                // the copies in flight, with the default limit
+                if (*abort || !ws_wait(&empty[s], n & 1, abort, lim)) mbar_wait(&full[s], n & 1);
             }
         }
     } else if (warp == 1) {
         if (lane == 0) {
             // MMA issuer
+            // abort test: wait on the drain barrier, which nothing completes
+            // before the MMAs are drained, until the limit runs out
+            if (g.wait < 0) ws_wait(drain, 0, abort, -g.wait);
             const uint32_t idesc = umma_idesc(GM_BM, N);
             uint32_t it = 0;
             int lu = 0;
@@ -462,14 +472,14 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
                 const int k_lo = ks * w.k_per_split, k_hi = min(K, k_lo + w.k_per_split);
                 const int acc = lu & 1;
                 const uint32_t na = (uint32_t)(lu >> 1);
-                if (na > 0 && !ws_wait(&acc_empty[acc], (na - 1) & 1, abort)) { ok = false; break; }
+                if (na > 0 && !ws_wait(&acc_empty[acc], (na - 1) & 1, abort, lim)) { ok = false; break; }
                 asm volatile("tcgen05.fence::after_thread_sync;");
                 const uint32_t d = tmem + (uint32_t)(acc * N);
                 bool first = true;
                 for (int k0 = k_lo; k0 < k_hi; k0 += GM_BK, ++it) {
                     const int s = it % WS_STAGES;
                     const uint32_t n = it / WS_STAGES;
-                    if (!ws_wait(&full[s], n & 1, abort)) { ok = false; break; }
+                    if (!ws_wait(&full[s], n & 1, abort, lim)) { ok = false; break; }
                     asm volatile("tcgen05.fence::after_thread_sync;");
                     const int kw = min(GM_BK, k_hi - k0);
                     const uint32_t a0 = sbase + s * WS_STAGE_BYTES, b0 = a0 + WS_A_BYTES;
@@ -512,7 +522,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
             const int acc = lu & 1;
             // lane 0 waits; the decision is warp-uniform (tcgen05.ld is .sync.aligned)
             int ok = 1;
-            if (lane == 0) ok = ws_wait(&acc_full[acc], (uint32_t)(lu >> 1) & 1, abort) ? 1 : 0;
+            if (lane == 0) ok = ws_wait(&acc_full[acc], (uint32_t)(lu >> 1) & 1, abort, lim) ? 1 : 0;
             if (!__shfl_sync(0xffffffffu, ok, 0)) break;
             asm volatile("tcgen05.fence::after_thread_sync;");
             if (active) {
@@ -1421,7 +1431,7 @@ int fdadi_mlp_gemm(const fdadi_gemm_t *a, void *stream) {
     GemmArgs g{(const bf16 *)a->A, a->lda, a->strideA, (const bf16 *)a->B, a->ldb, a->strideB,
                a->bias, a->strideBias, a->aux, a->ldaux, a->strideAux, a->out_f32, a->ldo,
                a->strideO, (bf16 *)a->out_bf16, a->ldh, a->strideH, a->M, a->N, a->K, a->act,
-               a->status};
+               a->status, (long long)a->wait_cycles};
     if (a->variant == 0) return launch_ws(a, g, as_stream(stream));
     dim3 grid(a->M / 128, a->problems);
     umma_gemm_kernel<<<grid, GM_THREADS, GM_SMEM, as_stream(stream)>>>(g);

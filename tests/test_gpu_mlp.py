@@ -20,14 +20,14 @@ def lib():
 
 
 def _gemm(L, A, B, M, N, K, problems=1, sA=0, sB=0, bias=None, sBias=0, aux=None, act=0,
-          out_f32=None, out_bf16=None, status=None, variant=0):
+          out_f32=None, out_bf16=None, status=None, variant=0, wait_cycles=0):
     g = L.Gemm(A.data_ptr(), A.shape[-1], sA, B.data_ptr(), B.shape[-1], sB,
                bias.data_ptr() if bias is not None else None, sBias,
                aux.data_ptr() if aux is not None else None, N, M * N,
                out_f32.data_ptr() if out_f32 is not None else None, N, M * N,
                out_bf16.data_ptr() if out_bf16 is not None else None, N, M * N,
                M, N, K, act, problems, variant,
-               status.data_ptr() if status is not None else None)
+               status.data_ptr() if status is not None else None, wait_cycles)
     L.call("fdadi_mlp_gemm", ctypes.byref(g),
            ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
 
@@ -143,3 +143,27 @@ def test_transpose_and_adam(lib):
     assert (p - ref).abs().max().item() < 1e-6
     assert torch.equal(w, p.to(torch.bfloat16))
     assert torch.equal(wt.view(cols, rows), p.to(torch.bfloat16).view(rows, cols).T)
+
+
+def test_bounded_wait_gives_up_and_context_stays_usable(lib):
+    """The warp-specialised GEMM's abort path: its MMA warp waits on a barrier
+    that nothing completes (wait_cycles < 0) until the limit (about 0.1 ms)
+    runs out; the kernel must drain its copies and MMAs, free its tensor
+    memory, set the status word and return. A normal launch afterwards on the
+    same stream gives the right result, twice."""
+    M, N, K = 256, 128, 256
+    gen = torch.Generator(device="cpu").manual_seed(9)
+    A = torch.randn(M, K, generator=gen).to(torch.bfloat16).cuda()
+    B = torch.randn(N, K, generator=gen).to(torch.bfloat16).cuda()
+    ref = A.float() @ B.float().T
+    for _ in range(2):
+        C = torch.zeros(M, N, dtype=torch.float32, device="cuda")
+        st = torch.zeros(1, dtype=torch.int32, device="cuda")
+        _gemm(lib, A, B, M, N, K, out_f32=C, status=st, variant=0, wait_cycles=-200000)
+        torch.cuda.synchronize()
+        assert int(st.item()) == 1
+        st.zero_()
+        _gemm(lib, A, B, M, N, K, out_f32=C, status=st, variant=0)
+        torch.cuda.synchronize()
+        assert int(st.item()) == 0
+        assert (C - ref).abs().max().item() <= 1e-4 * ref.abs().max().item()
