@@ -79,7 +79,8 @@ class HestonBatch(ctypes.Structure):
                 ("n0", ctypes.c_void_p), ("n1", ctypes.c_void_p),
                 ("spots", ctypes.c_void_p), ("vars", ctypes.c_void_p),
                 ("params", ctypes.c_void_p), ("dt", ctypes.c_void_p),
-                ("barrier", ctypes.c_void_p), ("plan", ctypes.c_void_p)]
+                ("barrier", ctypes.c_void_p), ("plan", ctypes.c_void_p),
+                ("rates", ctypes.c_void_p)]
 
 
 class Gemm(ctypes.Structure):
@@ -92,7 +93,7 @@ class Gemm(ctypes.Structure):
                 ("out_bf16", ctypes.c_void_p), ("ldh", ctypes.c_int64), ("strideH", ctypes.c_int64),
                 ("M", ctypes.c_int32), ("N", ctypes.c_int32), ("K", ctypes.c_int32),
                 ("act", ctypes.c_int32), ("problems", ctypes.c_int32), ("variant", ctypes.c_int32),
-                ("status", ctypes.c_void_p)]
+                ("status", ctypes.c_void_p), ("wait_cycles", ctypes.c_int64)]
 
 
 # name -> (restype, argtypes); every symbol include/fdadi.h declares

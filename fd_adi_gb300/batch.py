@@ -95,11 +95,15 @@ class HestonBatch(object):
     then ``n_steps`` of ``scheme`` ("douglas", "hv", "cs" or "mcs") at ``theta``.
     plan:    launch plan of the line solves: None (size heuristic), "auto"
              (measured by the autotuner on this batch, cached by batch shape)
-             or a dict of fdadi_heston_plan_t fields."""
+             or a dict of fdadi_heston_plan_t fields.
+    rates:   time-dependent coefficients: [n, implicit_steps + n_steps] interest
+             rate of every step of every option (the implicit steps first), or
+             None to use each option's constant r. With rates, the operators and
+             line-solve factors are rebuilt before every step."""
 
     def __init__(self, options, meshes, scheme="hv", n_steps=1, dt=0.01, theta=HV_THETA,
                  implicit_steps=0, implicit_dt_factor=0.5, barrier=None, drop_zero_mixed=True,
-                 graph=False, device=None, stream=None, plan=None):
+                 graph=False, device=None, stream=None, plan=None, rates=None):
         self.device = device or torch.device("cuda", torch.cuda.current_device())
         n = len(options)
         if n == 0 or len(meshes) != n:
@@ -122,6 +126,14 @@ class HestonBatch(object):
                                   device=dev)
         bar = np.zeros(n, dtype=np.int32) if barrier is None else np.asarray(barrier, np.int32)
         self.barrier = torch.as_tensor(bar, device=dev)
+        self.rates = None
+        if rates is not None:
+            total = int(implicit_steps) + int(n_steps)
+            r = np.ascontiguousarray(rates, dtype=np.float64)
+            if r.shape != (n, total):
+                raise ValueError("rates must have shape (%d, %d) (options, implicit_steps + "
+                                 "n_steps), got %s" % (n, total, r.shape))
+            self.rates = torch.as_tensor(r, device=dev)
         self.graph = bool(graph)
         if stream is None:
             stream = torch.cuda.Stream(device=dev) if self.graph else torch.cuda.current_stream(dev)
@@ -135,7 +147,8 @@ class HestonBatch(object):
             float(implicit_dt_factor), flags, 0,
             self._n0_host.ctypes.data, self._n1_host.ctypes.data,
             self.spots.data_ptr(), self.vars.data_ptr(), self.params.data_ptr(),
-            self.dt.data_ptr(), self.barrier.data_ptr(), None)
+            self.dt.data_ptr(), self.barrier.data_ptr(), None,
+            self.rates.data_ptr() if self.rates is not None else None)
         self._plan = None
         lib = _lib.load()
         nbytes = lib.fdadi_heston_workspace_bytes(ctypes.byref(self.struct))

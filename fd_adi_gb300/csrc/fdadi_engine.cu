@@ -227,27 +227,39 @@ struct BuildArgs {
     int smoothing;     // nonzero: build the implicit plan too
     int drop_zero_mixed;
     int hv;            // nonzero: build the HV corrector's scaled copies too
+    const double *rates = nullptr;  // per-step r ([n_opt][rate_stride]) or null
+    int64_t rate_stride = 0;
+    int rate_step = 0;              // the step whose r the build uses
 };
 
 __device__ __forceinline__ void opt_params(const BuildArgs &a, int o, double &r, double &kappa,
                                            double &th, double &sigma, double &rho) {
     const double *p = a.params + 5 * (int64_t)o;
-    r = p[0]; kappa = p[1]; th = p[2]; sigma = p[3]; rho = p[4];
+    r = a.rates ? a.rates[(int64_t)o * a.rate_stride + a.rate_step] : p[0];
+    kappa = p[1]; th = p[2]; sigma = p[3]; rho = p[4];
 }
 
 // Thomas factors (a_k, 1/m_k, c'_k) of one line with rows (sub, mid, sup):
 // m_0 = mid_0, m_k = mid_k - sub_k c'_{k-1}, c'_k = sup_k / m_k; stored at
 // L[q], L[stride + q], L[2 stride + q].
 // bad: some pivot m_k was zero or non-finite.
+// The factors are formed with the elimination's own operations, each rounded
+// once (m = mid - sub c' without a fused multiply-add, c' = sup / m by true
+// division), as the reference's banded solve forms them. They are built once
+// and reused by every solve of the run, so a factor rounded differently (c' as
+// sup times the rounded 1/m) would bias every step the same way: over 1000
+// steps of the 1024 x 512 grid that drift reached 1.4e-10 of the price. The
+// time loop multiplies by the stored 1/m, whose rounding does not accumulate
+// that way.
 struct Thomas {
     double cp = 0.0;
     bool bad = false;
     __device__ __forceinline__ void row(double *L, int64_t stride, int64_t q, double sub, double mid,
                                         double sup, bool first) {
-        const double m = first ? mid : mid - sub * cp;
-        const double inv = 1.0 / m;
+        const double m = first ? mid : SUB(mid, MUL(sub, cp));
+        const double inv = DIV(1.0, m);
         if (!isfinite(inv)) bad = true;
-        cp = sup * inv;
+        cp = DIV(sup, m);
         L[q] = sub;
         L[stride + q] = inv;
         L[2 * stride + q] = cp;
@@ -1544,6 +1556,8 @@ static int grids(const fdadi_heston_batch_t *b, const Layout &L, Grids &g) {
     FDADI_REQUIRE(p.groups >= 0 && p.groups <= MAX_GROUPS, "plan groups must be 0..%d (%d)",
                   MAX_GROUPS, p.groups);
     g.groups = std::max(1, std::min<int>(p.groups, L.n_opt));
+    // per-step rebuilds run on the batch's stream between whole steps
+    if (b->rates) g.groups = 1;
     g.corr = b->scheme == FDADI_SCHEME_CS ? ST_CS3 : b->scheme == FDADI_SCHEME_MCS ? ST_MCS3 : ST_HV3;
     FDADI_REQUIRE(p.expl_per_sm >= 0 && p.expl_per_sm <= 4,
                   "plan expl_per_sm must be 0..4 (%d)", p.expl_per_sm);
@@ -1679,6 +1693,32 @@ struct EventSet {
     }
 };
 
+// The per-option scalars, the per-point operator rows and the spot-line
+// factors (everything that depends on r; the spot stencil weights do not).
+static int launch_build(const Layout &L, const Arena &A, const BuildArgs &a, cudaStream_t st) {
+    build_options_kernel<<<(unsigned)((L.n_opt + 127) / 128), 128, 0, st>>>(A, a);
+    FDADI_CHECK_LAUNCH();
+    build_points_kernel<<<(unsigned)L.n_tiles, EXPL_THREADS, 0, st>>>(A, a);
+    FDADI_CHECK_LAUNCH();
+    build_spot_lines_kernel<<<(unsigned)((L.SV + 127) / 128), 128, 0, st>>>(A, a);
+    FDADI_CHECK_LAUNCH();
+    return FDADI_OK;
+}
+
+// Build arguments of this batch; with per-step rates, the builds of `step`.
+static BuildArgs build_args(const fdadi_heston_batch_t *b, const Layout &L, int step) {
+    BuildArgs a{b->spots, b->vars, b->params, b->dt, b->barrier, b->theta, b->implicit_dt_factor,
+                L.smoothing ? 1 : 0, (b->flags & FDADI_HESTON_DROP_ZERO_MIXED) ? 1 : 0,
+                L.hv ? 1 : 0};
+    if (b->rates) {
+        a.rates = b->rates;
+        a.rate_stride = (int64_t)b->implicit_steps + b->n_steps;
+        a.rate_step = step;
+    }
+    return a;
+}
+
+
 static void phases_of(const fdadi_heston_batch_t *b, std::vector<int> &ph) {
     for (int s = 0; s < b->implicit_steps; ++s) ph.push_back(PH_IMPLICIT);
     for (int s = 0; s < b->n_steps; ++s) {
@@ -1705,7 +1745,16 @@ static int launch_steps(const fdadi_heston_batch_t *b, const Layout &L, const Ar
     std::vector<int> ph;
     phases_of(b, ph);
     if (g.groups == 1) {
-        for (int kind : ph) launch_phase(kind, g, g.all, A, V, st, 0);
+        int step = 0;
+        for (int kind : ph) {
+            // time-dependent coefficients: rebuild before the step's first phase
+            if (b->rates && kind != PH_HV_CORRECT) {
+                rc = launch_build(L, A, build_args(b, L, step), st);
+                if (rc) return rc;
+                ++step;
+            }
+            launch_phase(kind, g, g.all, A, V, st, 0);
+        }
         FDADI_CHECK_LAUNCH();
         return FDADI_OK;
     }
@@ -1763,8 +1812,9 @@ struct GraphKey {
     const void *ws; const void *V; int n_opt, scheme, n_steps, smoothing;
     int64_t P, SS, SV, n_tiles, n_vtasks;
     int si, vi, groups;
+    const void *rates;
     bool operator==(const GraphKey &o) const {
-        return ws == o.ws && V == o.V && n_opt == o.n_opt && scheme == o.scheme &&
+        return ws == o.ws && V == o.V && n_opt == o.n_opt && scheme == o.scheme && rates == o.rates &&
                n_steps == o.n_steps && smoothing == o.smoothing && P == o.P && SS == o.SS &&
                SV == o.SV && n_tiles == o.n_tiles && n_vtasks == o.n_vtasks && si == o.si &&
                vi == o.vi && groups == o.groups;
@@ -1804,10 +1854,12 @@ int64_t fdadi_heston_workspace_bytes(const fdadi_heston_batch_t *batch) {
 int64_t fdadi_heston_launch_count(const fdadi_heston_batch_t *b) {
     if (!b) return -1;
     int64_t groups = 1;
-    if (b->plan && b->plan->groups > 1)
+    if (b->plan && b->plan->groups > 1 && !b->rates)
         groups = std::min<int64_t>(std::min(b->plan->groups, MAX_GROUPS), b->n_options);
-    return groups * ((int64_t)3 * b->implicit_steps +
-                     (int64_t)b->n_steps * (b->scheme == FDADI_SCHEME_DOUGLAS ? 3 : 6));
+    // time-dependent coefficients: three build launches before every step
+    const int64_t rebuild = b->rates ? (int64_t)3 * (b->implicit_steps + b->n_steps) : 0;
+    return rebuild + groups * ((int64_t)3 * b->implicit_steps +
+                               (int64_t)b->n_steps * (b->scheme == FDADI_SCHEME_DOUGLAS ? 3 : 6));
 }
 
 int fdadi_heston_prepare(const fdadi_heston_batch_t *b, void *workspace, int64_t ws_bytes,
@@ -1847,17 +1899,11 @@ int fdadi_heston_prepare(const fdadi_heston_batch_t *b, void *workspace, int64_t
     FDADI_CUDA(cudaMemcpyAsync(ws + L.o_theta, theta.data(), 8 * L.n_opt, cudaMemcpyHostToDevice, st));
     FDADI_CUDA(cudaMemsetAsync(ws + L.o_ostat, 0, 4 * L.n_opt, st));
     Arena A = arena_view(L, ws);
-    BuildArgs a{b->spots, b->vars, b->params, b->dt, b->barrier, b->theta, b->implicit_dt_factor,
-                L.smoothing ? 1 : 0, (b->flags & FDADI_HESTON_DROP_ZERO_MIXED) ? 1 : 0,
-                L.hv ? 1 : 0};
+    const BuildArgs a = build_args(b, L, 0);
     build_spot_weights_kernel<<<(unsigned)L.n_opt, 128, 0, st>>>(A, a);
     FDADI_CHECK_LAUNCH();
-    build_options_kernel<<<(unsigned)((L.n_opt + 127) / 128), 128, 0, st>>>(A, a);
-    FDADI_CHECK_LAUNCH();
-    build_points_kernel<<<(unsigned)L.n_tiles, EXPL_THREADS, 0, st>>>(A, a);
-    FDADI_CHECK_LAUNCH();
-    build_spot_lines_kernel<<<(unsigned)((L.SV + 127) / 128), 128, 0, st>>>(A, a);
-    FDADI_CHECK_LAUNCH();
+    rc = launch_build(L, A, a, st);
+    if (rc) return rc;
     // the host tables must outlive the copies
     FDADI_CUDA(cudaStreamSynchronize(st));
     return FDADI_OK;
@@ -1882,7 +1928,7 @@ int fdadi_heston_run(const fdadi_heston_batch_t *b, void *workspace, int64_t ws_
     rc = grids(b, L, g);
     if (rc) return rc;
     GraphKey key{workspace, V, b->n_options, b->scheme, b->n_steps, b->implicit_steps,
-                 L.P, L.SS, L.SV, L.n_tiles, L.n_vtasks, g.si, g.vi, g.groups};
+                 L.P, L.SS, L.SV, L.n_tiles, L.n_vtasks, g.si, g.vi, g.groups, b->rates};
     cudaGraphExec_t exec = nullptr;
     {
         std::lock_guard<std::mutex> g(g_graph_mu);

@@ -70,6 +70,11 @@ class FiniteDifferenceEngine(object):
         self.zero_derivative_f32 = True
         self.implicit_residual = True
         self.gpugrid = None
+        # time-dependent coefficients: the interest rate of every step of the
+        # next solve (the implicit steps of solve_smooth first), or None
+        self.rates = None
+        self._rate = None
+        self._rate_step = 0
 
     @property
     def shape(self):
@@ -195,6 +200,46 @@ class FiniteDifferenceEngineADI(FiniteDifferenceEngine):
         return [(d, o) for d, o in sorted(self.operators.items(), key=lambda kv: str(kv[0]))
                 if not isinstance(d, tuple)]
 
+    def _next_rate(self):
+        """With per-step rates (self.rates): take the next step's rate and
+        rebuild the combined operators for it, as preprocess_operators is
+        meant to run per step for time-dependent parameters
+        (FiniteDifferenceEngineGPU.pyx:163-167). Returns True if it did."""
+        if self.rates is None:
+            return False
+        rates = np.asarray(self.rates, dtype=np.float64).reshape(-1)
+        if self._rate_step >= rates.size:
+            raise ValueError("rates holds %d steps; the solve needs more" % rates.size)
+        self._rate = float(rates[self._rate_step])
+        self._rate_step += 1
+        self.zero_derivative_coefficient_host = np.atleast_1d(-self._rate / self.grid.ndim)
+        self.operators = {}
+        self.scale_and_combine_operators()
+        return True
+
+    def _start_rates(self):
+        """Start of a solve: step 0 of self.rates. Operators left at the last
+        step's rate by an earlier time-dependent solve are dropped."""
+        self._rate_step = 0
+        if self._rate is not None:
+            self._rate = None
+            self.operators = {}
+            self.zero_derivative_coefficient_host = None
+
+    def _split_ops(self, dt, theta):
+        """Firsts, Les, Lis for one (dt, theta), folded where foldable."""
+        Firsts = [o.mul_scalar_from_host(dt) for d, o in self.operators.items()]
+        dims = self._dims()
+        Les = [o.mul_scalar_from_host(theta).mul_scalar_from_host(dt, inplace=True)
+               for d, o in dims]
+        Lis = [o.mul_scalar_from_host(theta * -dt).add(1, inplace=True) for d, o in dims]
+        for L in Les + Lis:
+            L.enable_residual(False)
+        for L in Les + Lis + Firsts:
+            if L.is_foldable():
+                L.diagonalize()
+        return Firsts, Les, Lis
+
     # -- host wrappers --
     def _initial(self, initial):
         if initial is not None:
@@ -205,6 +250,7 @@ class FiniteDifferenceEngineADI(FiniteDifferenceEngine):
         if callback or numpy:
             raise NotImplementedError("Callbacks and Numpy not available for GPU solver.")
         V = self._initial(initial)
+        self._start_rates()
         self.solve_implicit_(int(n), dt, V)
         return V.cpu().numpy()
 
@@ -212,6 +258,7 @@ class FiniteDifferenceEngineADI(FiniteDifferenceEngine):
         if callback or numpy:
             raise NotImplementedError("Callbacks and Numpy not available for GPU solver.")
         V = self._initial(initial)
+        self._start_rates()
         self.solve_douglas_(int(n), dt, V, theta)
         return V.cpu().numpy()
 
@@ -219,6 +266,7 @@ class FiniteDifferenceEngineADI(FiniteDifferenceEngine):
         if callback or numpy:
             raise NotImplementedError("Callbacks and Numpy not available for GPU solver.")
         V = self._initial(initial)
+        self._start_rates()
         self.solve_hundsdorferverwer_(int(n), dt, V, theta)
         return V.cpu().numpy()
 
@@ -226,6 +274,7 @@ class FiniteDifferenceEngineADI(FiniteDifferenceEngine):
         if scheme:
             raise NotImplementedError("Changing smoothing schemes not supported on GPU.")
         V = self._initial(initial)
+        self._start_rates()
         self.solve_smooth_(int(n), dt, V, smoothing_steps)
         return V.cpu().numpy()
 
@@ -238,17 +287,26 @@ class FiniteDifferenceEngineADI(FiniteDifferenceEngine):
         dt = float(dt)
         if not self.operators:
             self.scale_and_combine_operators()
-        Lis = [o.mul_scalar_from_host(-dt).add(1, inplace=True) for d, o in self._dims()]
-        for L in Lis:
-            L.enable_residual(self.implicit_residual and True)
-        Lis = Lis[1:] + Lis[:1]
-        cross = self.operators.get((0, 1))
-        cross = cross.mul_scalar_from_host(dt) if cross is not None else None
-        for L in Lis:
-            if L.is_foldable():
-                L.diagonalize()
+
+        def prep():
+            Lis = [o.mul_scalar_from_host(-dt).add(1, inplace=True) for d, o in self._dims()]
+            for L in Lis:
+                L.enable_residual(self.implicit_residual and True)
+            Lis = Lis[1:] + Lis[:1]
+            cross = self.operators.get((0, 1))
+            cross = cross.mul_scalar_from_host(dt) if cross is not None else None
+            for L in Lis:
+                if L.is_foldable():
+                    L.diagonalize()
+            return Lis, cross
+
+        timedep = self.rates is not None
+        if not timedep:
+            Lis, cross = prep()
         U = torch.empty_like(V)
         for _ in range(int(n)):
+            if timedep and self._next_rate():
+                Lis, cross = prep()
             if cross is not None:
                 _apply_into(cross, U, V)
                 _axpby(V, U, 1.0, 1.0)
@@ -261,19 +319,14 @@ class FiniteDifferenceEngineADI(FiniteDifferenceEngine):
         dt, theta = float(dt), float(theta)
         if not self.operators:
             self.scale_and_combine_operators()
-        Firsts = [o.mul_scalar_from_host(dt) for d, o in self.operators.items()]
-        dims = self._dims()
-        Les = [o.mul_scalar_from_host(theta).mul_scalar_from_host(dt, inplace=True)
-               for d, o in dims]
-        Lis = [o.mul_scalar_from_host(theta * -dt).add(1, inplace=True) for d, o in dims]
-        for L in Les + Lis:
-            L.enable_residual(False)
-        for L in Les + Lis + Firsts:
-            if L.is_foldable():
-                L.diagonalize()
+        timedep = self.rates is not None
+        if not timedep:
+            Firsts, Les, Lis = self._split_ops(dt, theta)
         Y = V.clone()
         X = torch.empty_like(V)
         for _ in range(int(n)):
+            if timedep and self._next_rate():
+                Firsts, Les, Lis = self._split_ops(dt, theta)
             for L in Firsts:
                 _apply_into(L, X, Y)
                 _axpby(V, X, 1.0, 1.0)
@@ -289,20 +342,15 @@ class FiniteDifferenceEngineADI(FiniteDifferenceEngine):
         dt, theta = float(dt), float(theta)
         if not self.operators:
             self.scale_and_combine_operators()
-        Firsts = [o.mul_scalar_from_host(dt) for d, o in self.operators.items()]
-        dims = self._dims()
-        Les = [o.mul_scalar_from_host(theta).mul_scalar_from_host(dt, inplace=True)
-               for d, o in dims]
-        Lis = [o.mul_scalar_from_host(theta * -dt).add(1, inplace=True) for d, o in dims]
-        for L in Les + Lis:
-            L.enable_residual(False)
-        for L in Les + Lis + Firsts:
-            if L.is_foldable():
-                L.diagonalize()
+        timedep = self.rates is not None
+        if not timedep:
+            Firsts, Les, Lis = self._split_ops(dt, theta)
         X = torch.empty_like(V)
         Y = torch.empty_like(V)
         Z = torch.empty_like(V)
         for _ in range(int(n)):
+            if timedep and self._next_rate():
+                Firsts, Les, Lis = self._split_ops(dt, theta)
             Y.copy_(V)
             for L in Firsts:
                 _apply_into(L, X, Y)
@@ -471,6 +519,8 @@ class HestonFiniteDifferenceEngine(FiniteDifferenceEngineADI):
         """Per-point Heston coefficients in the operator's block-major order
         (heston.py:303-325; GPU: _coefficients.cu:19-115)."""
         r, kappa, theta, sigma, rho = self.option.params()
+        if self._rate is not None:
+            r = self._rate          # this step's rate (time-dependent coefficients)
         S, v = self.spots, self.vars
         if dim == 0:
             Sg, vg = np.meshgrid(S, v)          # [nv, nS]: spot fastest
@@ -505,9 +555,16 @@ class HestonFiniteDifferenceEngine(FiniteDifferenceEngineADI):
     # -- fused path --
     def _batch(self, scheme, n_steps, dt, theta, implicit_steps=0, factor=0.5):
         from .batch import HestonBatch
+        rates = None
+        if self.rates is not None:
+            total = int(implicit_steps) + int(n_steps)
+            r = np.asarray(self.rates, dtype=np.float64).reshape(-1)
+            if r.size < total:
+                raise ValueError("rates holds %d steps; the solve needs %d" % (r.size, total))
+            rates = r[:total].reshape(1, total)
         return HestonBatch([self.option], [(self.spots, self.vars)], scheme=scheme,
                            n_steps=n_steps, dt=[dt], theta=theta, implicit_steps=implicit_steps,
-                           implicit_dt_factor=factor, barrier=[bool(self.barrier)])
+                           implicit_dt_factor=factor, barrier=[bool(self.barrier)], rates=rates)
 
     def _fused_run(self, initial, scheme, n_steps, dt, theta, implicit_steps=0, factor=0.5):
         V0 = self.grid.domain[-1] if initial is None else initial

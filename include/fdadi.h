@@ -219,6 +219,14 @@ typedef struct fdadi_heston_batch {
     const double *dt;        /* DEVICE [n_options] main-segment step */
     const int32_t *barrier;  /* DEVICE [n_options] nonzero: up-and-out (Dirichlet 0 at S_max), or NULL */
     const fdadi_heston_plan_t *plan; /* HOST launch plan of the line solves, or NULL (heuristic) */
+    const double *rates;     /* DEVICE [n_options][implicit_steps + n_steps] interest rate of
+                              * every step (time-dependent coefficients), or NULL: params' r.
+                              * Step k (the implicit steps first) uses rates[o][k] wherever r
+                              * enters the operators (the drift r S, the -r/2 split, the S_max
+                              * residual); the operators and line-solve factors are rebuilt
+                              * before every step, as preprocess_operators is documented to be
+                              * run per step for time-dependent parameters
+                              * (FiniteDifferenceEngineGPU.pyx:163-167). */
 } fdadi_heston_batch_t;
 
 /* drop the mixed operator of options with rho == 0, as the GPU reference
@@ -344,6 +352,13 @@ typedef struct fdadi_gemm {
                         * atomic adds when there are few output tiles and no epilogue);
                         * 1: one CTA per tile, two cp.async stages */
     int32_t *status;
+    int64_t wait_cycles;  /* variant 0: clock cycles after which a wait on a copy,
+                           * an MMA or an epilogue gives up (0: about 2 s). The
+                           * kernel then drains the copies and MMAs it issued,
+                           * frees its tensor memory, sets *status and returns.
+                           * Negative: a test of that path; the MMA warp first
+                           * waits -wait_cycles cycles on a barrier that nothing
+                           * completes, so the launch always aborts. */
 } fdadi_gemm_t;
 int fdadi_mlp_gemm(const fdadi_gemm_t *gemm, void *stream);
 

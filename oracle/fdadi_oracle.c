@@ -422,16 +422,23 @@ static void engine_free(engine_t *E) {
 
 /* Heston operators: coefficients heston.py:303-333, boundaries heston.py:335-359,
  * built as in make_discrete_operators and scale_and_combine_operators
- * (FiniteDifferenceEngine.pyx:423-592). */
+ * (FiniteDifferenceEngine.pyx:423-592). An up-and-out barrier at the top of
+ * the spot mesh makes the high boundary of both spot operators Dirichlet 0,
+ * and (0,0) takes (0,)'s boundaries (heston.py:361-370). */
 static void heston_engine(engine_t *E, const double *S, int nS, const double *v, int nv,
-                          double r, double kappa, double theta, double sigma, double rho) {
+                          double r, double kappa, double theta, double sigma, double rho,
+                          int barrier) {
     int N = nS * nv;
     E->ndim = 2; E->n0 = nS; E->n1 = nv;
     double *vec = (double *)malloc((size_t)N * sizeof(double));
-    /* (0,): D U=0 / Neumann dU/dS = 1 */
-    op_t *d0 = derivative_op(S, nS, nv, 0, 1, BND_DIRICHLET, 0.0, BND_NEUMANN, 1.0, 0);
-    /* (0,0): D U=0 / free, first derivative 1 */
-    op_t *d00 = derivative_op(S, nS, nv, 0, 2, BND_DIRICHLET, 0.0, BND_NONE, 1.0, 0);
+    /* (0,): D U=0 / Neumann dU/dS = 1 (barrier: D U=0) */
+    op_t *d0 = barrier
+        ? derivative_op(S, nS, nv, 0, 1, BND_DIRICHLET, 0.0, BND_DIRICHLET, 0.0, 0)
+        : derivative_op(S, nS, nv, 0, 1, BND_DIRICHLET, 0.0, BND_NEUMANN, 1.0, 0);
+    /* (0,0): D U=0 / free, first derivative 1 (barrier: D U=0) */
+    op_t *d00 = barrier
+        ? derivative_op(S, nS, nv, 0, 2, BND_DIRICHLET, 0.0, BND_DIRICHLET, 0.0, 0)
+        : derivative_op(S, nS, nv, 0, 2, BND_DIRICHLET, 0.0, BND_NONE, 1.0, 0);
     /* (1,): free / free */
     op_t *d1 = derivative_op(v, nv, nS, 1, 1, BND_NONE, NAN, BND_NONE, NAN, 0);
     /* (1,1): Neumann 0 / free second order (offset -2) */
@@ -707,18 +714,37 @@ static void run_schedule(const engine_t *E, int nseg, const int *scheme, const i
 
 /* One Heston solve on a given mesh. V: [nS*nv] initial grid in, final out.
  * Segments run in order: scheme 0 implicit, 1 Douglas, 2 Hundsdorfer-Verwer,
- * 3 Craig-Sneyd, 4 modified Craig-Sneyd. */
+ * 3 Craig-Sneyd, 4 modified Craig-Sneyd. flags: bit 0 drops the mixed
+ * operator when rho = 0, bit 1 makes the top of the spot mesh an up-and-out
+ * barrier. */
 int oracle_heston_solve(const double *S, int nS, const double *v, int nv,
                         double r, double kappa, double theta, double sigma, double rho,
-                        int drop_zero_mixed,
+                        int flags,
                         int nseg, const int *scheme, const int *nsteps,
-                        const double *dt, const double *th, double *V) {
+                        const double *dt, const double *th, double *V, const double *rates) {
     if (nS < 4 || nv < 4) return 1;
     engine_t E;
-    heston_engine(&E, S, nS, v, nv, r, kappa, theta, sigma, rho);
-    if (drop_zero_mixed && rho == 0) { op_free(E.M); E.M = NULL; }
-    run_schedule(&E, nseg, scheme, nsteps, dt, th, V);
-    engine_free(&E);
+    if (!rates) {
+        heston_engine(&E, S, nS, v, nv, r, kappa, theta, sigma, rho, (flags & 2) != 0);
+        if ((flags & 1) && rho == 0) { op_free(E.M); E.M = NULL; }
+        run_schedule(&E, nseg, scheme, nsteps, dt, th, V);
+        engine_free(&E);
+        return 0;
+    }
+    /* time-dependent coefficients: step k of the schedule (segments in order)
+     * runs on operators built with r = rates[k], the operators rebuilt before
+     * every step (what preprocess_operators is documented to do per step,
+     * FiniteDifferenceEngineGPU.pyx:163-167). */
+    int k = 0;
+    for (int sg = 0; sg < nseg; ++sg) {
+        for (int s = 0; s < nsteps[sg]; ++s, ++k) {
+            heston_engine(&E, S, nS, v, nv, rates[k], kappa, theta, sigma, rho, (flags & 2) != 0);
+            if ((flags & 1) && rho == 0) { op_free(E.M); E.M = NULL; }
+            const int one = 1;
+            run_schedule(&E, 1, scheme + sg, &one, dt + sg, th + sg, V);
+            engine_free(&E);
+        }
+    }
     return 0;
 }
 
@@ -744,7 +770,7 @@ int oracle_heston_operators(const double *S, int nS, const double *v, int nv,
                             int *status) {
     if (nS < 4 || nv < 4) return 1;
     engine_t E;
-    heston_engine(&E, S, nS, v, nv, r, kappa, theta, sigma, rho);
+    heston_engine(&E, S, nS, v, nv, r, kappa, theta, sigma, rho, 0);
     size_t N = (size_t)nS * nv;
     for (int k = 0; k < 5; ++k) {
         memcpy(A0 + k * N, E.A[0]->d[k], N * sizeof(double));
@@ -761,21 +787,26 @@ int oracle_heston_operators(const double *S, int nS, const double *v, int nv,
 
 /* A batch of independent Heston solves, one OpenMP thread per option. The
  * meshes and grids of option k start at S_off[k], v_off[k], V_off[k]; every
- * option runs the same segment list. */
+ * option runs the same segment list; barrier (may be NULL) marks up-and-out
+ * options. */
 int oracle_heston_batch(int n_opt, const double *S, const int64_t *S_off, const int *nS,
                         const double *v, const int64_t *v_off, const int *nv,
                         const double *params /* [n_opt][5]: r kappa theta sigma rho */,
                         int nseg, const int *scheme, const int *nsteps,
                         const double *dt /* [n_opt][nseg] */, const double *th,
-                        double *V, const int64_t *V_off, int nthreads) {
+                        double *V, const int64_t *V_off, int nthreads, const int *barrier,
+                        const double *rates /* [n_opt][total steps] or NULL */) {
     int bad = 0;
+    int total = 0;
+    for (int sg = 0; sg < nseg; ++sg) total += nsteps[sg];
 #pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads) reduction(+ : bad)
     for (int k = 0; k < n_opt; ++k) {
         const double *p = params + 5 * k;
         bad += oracle_heston_solve(S + S_off[k], nS[k], v + v_off[k], nv[k],
-                                   p[0], p[1], p[2], p[3], p[4], 1,
+                                   p[0], p[1], p[2], p[3], p[4],
+                                   1 | ((barrier && barrier[k]) ? 2 : 0),
                                    nseg, scheme, nsteps, dt + (size_t)k * nseg, th,
-                                   V + V_off[k]);
+                                   V + V_off[k], rates ? rates + (size_t)k * total : NULL);
     }
     return bad;
 }

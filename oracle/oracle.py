@@ -44,12 +44,12 @@ def lib():
         lp = ctypes.POINTER(ctypes.c_int64)
         c_int, c_d = ctypes.c_int, ctypes.c_double
         L.oracle_heston_solve.argtypes = [dp, c_int, dp, c_int, c_d, c_d, c_d, c_d, c_d, c_int,
-                                          c_int, ip, ip, dp, dp, dp]
+                                          c_int, ip, ip, dp, dp, dp, dp]
         L.oracle_bs_solve.argtypes = [dp, c_int, c_d, c_d, c_int, ip, ip, dp, dp, dp]
         L.oracle_heston_operators.argtypes = [dp, c_int, dp, c_int, c_d, c_d, c_d, c_d, c_d,
                                               dp, dp, dp, dp, dp, ip]
         L.oracle_heston_batch.argtypes = [c_int, dp, lp, ip, dp, lp, ip, dp, c_int, ip, ip,
-                                          dp, dp, dp, lp, c_int]
+                                          dp, dp, dp, lp, c_int, ip, dp]
         for f in (L.oracle_heston_solve, L.oracle_bs_solve, L.oracle_heston_operators,
                   L.oracle_heston_batch):
             f.restype = c_int
@@ -78,16 +78,20 @@ def _schedule(schedule):
     return sc, ns, dt, th
 
 
-def heston_solve(spots, vars_, r, kappa, theta, sigma, rho, V0, schedule, drop_zero_mixed=False):
-    """Run a schedule of ADI segments on the reference Heston operators."""
+def heston_solve(spots, vars_, r, kappa, theta, sigma, rho, V0, schedule, drop_zero_mixed=False,
+                 barrier=False, rates=None):
+    """Run a schedule of ADI segments on the reference Heston operators
+    (barrier: the top of the spot mesh is an up-and-out barrier; rates: the
+    interest rate of every step, the operators rebuilt before each)."""
     S = np.ascontiguousarray(spots, dtype=np.float64)
     v = np.ascontiguousarray(vars_, dtype=np.float64)
     V = np.array(V0, dtype=np.float64, order="C").copy()
     assert V.shape == (S.size, v.size)
     sc, ns, dt, th = _schedule(schedule)
     rc = lib().oracle_heston_solve(_dp(S), S.size, _dp(v), v.size, r, kappa, theta, sigma, rho,
-                                   int(drop_zero_mixed), len(sc), _ip(sc), _ip(ns), _dp(dt),
-                                   _dp(th), _dp(V))
+                                   int(bool(drop_zero_mixed)) | (2 if barrier else 0),
+                                   len(sc), _ip(sc), _ip(ns), _dp(dt),
+                                   _dp(th), _dp(V), _rates(rates, int(ns.sum())))
     if rc:
         raise ValueError("oracle_heston_solve failed (%d)" % rc)
     return V
@@ -120,12 +124,25 @@ def heston_operators(spots, vars_, r, kappa, theta, sigma, rho):
     return dict(A0=A0, R0=R0, A1=A1, R1=R1, M9=M9, status=st)
 
 
-def heston_batch(meshes, params, V0s, schedule_list, nthreads=None):
+def _rates(rates, total, n=None):
+    if rates is None:
+        return None
+    r = np.ascontiguousarray(rates, dtype=np.float64)
+    want = (total,) if n is None else (n, total)
+    if r.shape != want:
+        raise ValueError("rates must have shape %s, got %s" % (want, r.shape))
+    _rates.keep = r
+    return _dp(r)
+
+
+def heston_batch(meshes, params, V0s, schedule_list, nthreads=None, barriers=None, rates=None):
     """Price a list of options on the CPU, one thread per option.
 
     meshes: list of (spots, vars); params: [n,5] (r, kappa, theta, sigma, rho);
     V0s: list of initial grids; schedule_list: list (per option) of schedules
-    sharing schemes/nsteps/theta but with per-option dt."""
+    sharing schemes/nsteps/theta but with per-option dt; barriers: per option,
+    whether the top of its spot mesh is an up-and-out barrier; rates: [n, total
+    steps] per-step interest rates (time-dependent coefficients)."""
     n = len(meshes)
     nS = np.array([m[0].size for m in meshes], dtype=np.int32)
     nv = np.array([m[1].size for m in meshes], dtype=np.int32)
@@ -140,9 +157,12 @@ def heston_batch(meshes, params, V0s, schedule_list, nthreads=None):
     dt = np.array([[float(s[2]) for s in sch] for sch in schedule_list], dtype=np.float64)
     P = np.ascontiguousarray(params, dtype=np.float64)
     nthreads = int(nthreads or os.cpu_count() or 1)
+    bar = np.zeros(n, dtype=np.int32) if barriers is None else \
+        np.ascontiguousarray(barriers, dtype=np.int32)
     rc = lib().oracle_heston_batch(n, _dp(S), _lp(S_off), _ip(nS), _dp(v), _lp(v_off), _ip(nv),
                                    _dp(P), len(sc), _ip(sc), _ip(ns), _dp(dt), _dp(th), _dp(V),
-                                   _lp(V_off), nthreads)
+                                   _lp(V_off), nthreads, _ip(bar),
+                                   _rates(rates, int(ns.sum()), n))
     if rc:
         raise ValueError("oracle_heston_batch: %d options failed" % rc)
     return [V[V_off[k]:V_off[k] + sizes[k]].reshape(nS[k], nv[k]) for k in range(n)]

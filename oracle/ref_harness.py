@@ -60,8 +60,10 @@ def heston_mesh(S0, K, v0, nS, nv, spot_max, var_max, spotdensity=7.0, varexp=4.
     return spots, np.array(vars_, dtype=float)
 
 
-def heston_engine(S0, K, r, v0, kappa, theta, sigma, rho, spots, vars_):
-    """A reference FiniteDifferenceEngineADI with the Heston PDE (heston.py:302-359)."""
+def heston_engine(S0, K, r, v0, kappa, theta, sigma, rho, spots, vars_, barrier=False):
+    """A reference FiniteDifferenceEngineADI with the Heston PDE (heston.py:302-359);
+    barrier: an up-and-out barrier at the top of the spot mesh, whose spot
+    boundaries become Dirichlet 0 at both ends (heston.py:361-370)."""
     FD, BO, U, Grid = _import()
 
     def mu_s(t, *dim):
@@ -97,6 +99,9 @@ def heston_engine(S0, K, r, v0, kappa, theta, sigma, rho, spots, vars_):
         (1,): ((None, lambda t, *dim: None), (None, lambda t, *dim: None)),
         (1, 1): ((1, lambda t, *dim: 0), (None, lambda t, *dim: None)),
     }
+    if barrier:
+        boundaries[(0,)] = (boundaries[(0,)][0], (0, lambda *x: 0.0))
+        boundaries[(0, 0)] = boundaries[(0,)]
     schemes = {(0,): [{"scheme": "center"}], (1,): [{"scheme": "center"}]}
     grid = Grid([spots, vars_], initializer=lambda *x: np.maximum(x[0] - K, 0))
     F = FD.FiniteDifferenceEngineADI(grid, coefficients=coefficients,

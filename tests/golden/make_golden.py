@@ -165,6 +165,58 @@ def heston1024x512_short():
                         rowsum=V.sum(axis=1), colsum=V.sum(axis=0))
 
 
+def barrier():
+    """Up-and-out call, the reference's barrier test case
+    (tests/test_HestonBarrierOptionGPU.py:26-117): S0 = K = 100, r = 0.06,
+    v0 = 0.04, T = 1, kappa = 1, theta = 0.12, sigma = 0.3, rho = 0.4, barrier
+    170; 150 spots from exponential_space(0, K, 170, 1/3) and 80 variances to
+    the engine's default v_max = 10 (heston.py:276-296, 380-400); the high spot
+    boundary is Dirichlet 0 (heston.py:361-370). Implicit: 600 steps of 1/600;
+    Douglas and HV (theta 0.5): 150 steps of 1/150; smooth: 4 implicit
+    half-steps then 148 HV steps at theta 0.6 (solve_smooth's defaults)."""
+    FD, BO, U, Grid = H._import()
+    K, S0, v0, B = 100., 100., 0.04, 170.
+    S = np.array(H.quiet(U.exponential_space, 0.0, K, B, 1.0 / 3, 150, force_exact=True))
+    v = np.array(H.quiet(U.exponential_space, 0.0, v0, 10.0, 4.0, 80, force_exact=True))
+    S[np.argmin(np.abs(S - S0))] = S0
+    params = (0.06, 1.0, 0.12, 0.3, 0.4)
+    F = H.heston_engine(S0, K, params[0], v0, params[1], params[2], params[3], params[4], S, v,
+                        barrier=True)
+    V0 = F.grid.domain[-1].copy()
+    out = dict(S=S, v=v, V0=V0, params=np.array(params), barrier=np.array(B))
+    out["implicit"] = H.quiet(F.solve_implicit, 600, 1.0 / 600, initial=V0)
+    out["douglas"] = H.quiet(F.solve_douglas, 150, 1.0 / 150, initial=V0, theta=0.5)
+    out["hv"] = H.quiet(F.solve_hundsdorferverwer, 150, 1.0 / 150, initial=V0, theta=0.5)
+    out["smooth"] = H.quiet(F.solve_smooth, 150, 1.0 / 150, initial=V0)
+    idx = H.price_index(S, v, S0, v0)
+    out["idx"] = np.array(idx)
+    np.savez_compressed(os.path.join(HERE, "barrier.npz"), **out)
+
+
+def heston1024x512_nt1000(cached=None):
+    """The large single grid in full: 1024x512, rho=-0.7, sigma=0.5, K=100,
+    two implicit half-steps then 999 HV steps (theta=1/2+sqrt(3)/6), dt=1/1000
+    (about 4 minutes of the reference engine). Stores the meshes, the price, a
+    down-sampled grid and whole-grid checksums. `cached`: an npz with the
+    reference's final grid Vr from an earlier run of exactly this."""
+    S, v = H.heston_mesh(100., 100., 0.04, 1024, 512, 800., 5.)
+    if cached:
+        d = np.load(cached)
+        assert np.array_equal(d["S"], S) and np.array_equal(d["v"], v)
+        V = d["Vr"]
+    else:
+        F = H.heston_engine(100., 100., 0.06, 0.04, 1.0, 0.04, 0.5, -0.7, S, v)
+        V0 = F.grid.domain[-1].copy()
+        dt = 1.0 / 1000
+        V = H.quiet(F.solve_implicit, 2, dt * 0.5, initial=V0)
+        V = H.quiet(F.solve_hundsdorferverwer, 999, dt, initial=V, theta=HV_THETA)
+    idx = H.price_index(S, v, 100., 0.04)
+    np.savez_compressed(os.path.join(HERE, "heston1024x512_nt1000.npz"), S=S, v=v,
+                        V_sub=V[::16, ::8], price=np.array(V[idx]), idx=np.array(idx),
+                        sum=np.array(V.sum()), rowsum=V.sum(axis=1), colsum=V.sum(axis=0),
+                        vmax=np.array(np.abs(V).max()))
+
+
 def blackscholes():
     """1-D Black-Scholes, the reference test case (tests/test_BlackScholesOption.py:24-75):
     S=100, K=99, r=0.06, var=0.04, T=1, 150 spots to 5000 with density 1."""
@@ -197,6 +249,8 @@ if __name__ == "__main__":
     heston150()
     heston1024x512_short()
     blackscholes()
+    barrier()
+    heston1024x512_nt1000(os.environ.get("FDADI_CFG2_CACHE"))
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

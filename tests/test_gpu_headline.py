@@ -91,13 +91,16 @@ def test_batched_workload_sizes_vs_oracle(cuda):
         assert _grid_rel(got[k], grid) <= GRID_BAR, (sizes[k], _grid_rel(got[k], grid))
 
 
-def test_large_single_instance_nt1000_vs_oracle(cuda):
+def test_large_single_instance_nt1000_vs_reference(cuda, golden):
     """1024 x 512, nt = 1000 (two implicit half-steps, then 999 HV steps at
-    theta = 1/2 + sqrt(3)/6), rho = -0.7, sigma = 0.5, K = 100, tuned plan."""
-    from fd_adi_gb300 import mesh
+    theta = 1/2 + sqrt(3)/6), rho = -0.7, sigma = 0.5, K = 100, tuned plan,
+    against the reference engine's own result (price, a down-sampled grid,
+    row and column sums) and the oracle's full grid, on the reference's
+    meshes."""
     from fd_adi_gb300.batch import HestonBatch
-    K, v0 = 100.0, 0.04
-    S, v = mesh.heston_meshes(100.0, K, v0, 1024, 512, 8.0 * K, 5.0)
+    g = golden("heston1024x512_nt1000")
+    S, v = g["S"], g["v"]
+    K = 100.0
     p = (0.06, 1.0, 0.04, 0.5, -0.7)
     nt, T = 1000, 1.0
     dt = T / nt
@@ -105,8 +108,13 @@ def test_large_single_instance_nt1000_vs_oracle(cuda):
                     implicit_steps=2, implicit_dt_factor=0.5, graph=True, plan="auto")
     V0 = np.maximum(S[:, None] - K, 0.0) * np.ones((1, v.size))
     got = b.solve([V0])[0]
+    i, j = g["idx"]
+    assert _price_bar_ok(got[i, j], float(g["price"])), (got[i, j], float(g["price"]))
+    vmax = float(g["vmax"])
+    assert np.abs(got[::16, ::8] - g["V_sub"]).max() <= GRID_BAR * vmax
+    np.testing.assert_allclose(got.sum(axis=1), g["rowsum"], rtol=1e-10, atol=1e-9 * vmax)
+    np.testing.assert_allclose(got.sum(axis=0), g["colsum"], rtol=1e-10, atol=1e-9 * vmax)
     ref = O.heston_solve(S, v, *p, V0, [("implicit", 2, dt / 2, 1.0),
                                         ("hv", nt - 1, dt, HV_THETA)])
-    i, j = mesh.price_index(S, v, 100.0, v0)
     assert _price_bar_ok(got[i, j], ref[i, j]), (got[i, j], ref[i, j])
     assert _grid_rel(got, ref) <= GRID_BAR, _grid_rel(got, ref)

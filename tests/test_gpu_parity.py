@@ -159,21 +159,69 @@ def test_graph_mode_matches_direct(cuda):
     np.testing.assert_array_equal(again, direct)
 
 
-def test_barrier_option_vs_host_engine(cuda):
-    """Up-and-out: Dirichlet 0 at the barrier (heston.py:361-370); fused path vs
-    the per-operator path on the same mesh."""
-    from fd_adi_gb300 import HestonBarrierOption, HestonFiniteDifferenceEngine
-    o = HestonBarrierOption(spot=100., strike=100., interest_rate=0.03, variance=0.04, tenor=0.5,
-                            mean_reversion=1.5, mean_variance=0.04, vol_of_variance=0.3,
-                            correlation=-0.3, top=(False, 170.))
-    F = HestonFiniteDifferenceEngine(o, nspots=60, nvols=30, var_max=5.0)
-    G = HestonFiniteDifferenceEngine(o, nspots=60, nvols=30, var_max=5.0, fused=False)
-    a = F.solve_hundsdorferverwer(25, 0.02, theta=HV_THETA)
-    b_ = G.solve_hundsdorferverwer(25, 0.02, theta=HV_THETA)
-    assert _rel(a, b_) < 1e-11
-    # the barrier row is forced to 0 by every spot solve; the variance solve
-    # that ends each step leaves it at rounding level, as in the reference
-    assert np.abs(a[-1]).max() < 1e-12 * np.abs(a).max()
+BARRIER_SCHED = {
+    "implicit": [("implicit", 600, 1.0 / 600, 1.0)],
+    "douglas": [("douglas", 150, 1.0 / 150, 0.5)],
+    "hv": [("hv", 150, 1.0 / 150, 0.5)],
+    "smooth": [("implicit", 4, 1.0 / 300, 1.0), ("hv", 148, 1.0 / 150, 0.6)],
+}
+BARRIER_BATCH = {
+    "implicit": dict(scheme="douglas", n_steps=0, dt=1.0 / 600, theta=0.5, implicit_steps=600,
+                     implicit_dt_factor=1.0),
+    "douglas": dict(scheme="douglas", n_steps=150, dt=1.0 / 150, theta=0.5),
+    "hv": dict(scheme="hv", n_steps=150, dt=1.0 / 150, theta=0.5),
+    "smooth": dict(scheme="hv", n_steps=148, dt=1.0 / 150, theta=0.6, implicit_steps=4,
+                   implicit_dt_factor=0.5),
+}
+
+
+def _barrier_option():
+    from fd_adi_gb300 import HestonBarrierOption
+    # the reference's barrier test case (tests/test_HestonBarrierOptionGPU.py:26-40)
+    return HestonBarrierOption(spot=100, strike=100, interest_rate=0.06, volatility=0.2,
+                               tenor=1.0, mean_reversion=1, mean_variance=0.12,
+                               vol_of_variance=0.3, correlation=0.4, top=(False, 170.0))
+
+
+@pytest.mark.parametrize("scheme", sorted(BARRIER_SCHED))
+def test_barrier_fused_vs_reference_and_oracle(cuda, golden, scheme):
+    """Up-and-out call (rho = 0.4, theta = 0.12, barrier 170, 150 x 80): the
+    fused batch with the barrier flag against the reference engine's grid and
+    the oracle, 1e-11 of the grid's max-norm."""
+    from fd_adi_gb300.batch import HestonBatch
+    g = golden("barrier")
+    S, v, V0 = g["S"], g["v"], g["V0"]
+    p = tuple(g["params"])
+    b = HestonBatch([p], [(S, v)], barrier=[1], **BARRIER_BATCH[scheme])
+    got = b.solve([V0])[0]
+    ref = g[scheme]
+    orc = O.heston_solve(S, v, *p, V0, BARRIER_SCHED[scheme], barrier=True)
+    assert _rel(got, ref) < 1e-11
+    assert _rel(got, orc) < 1e-11
+    i, j = g["idx"]
+    assert abs(got[i, j] - ref[i, j]) <= 1e-10 * abs(ref[i, j])
+    assert np.abs(got[-1]).max() <= 1e-12 * np.abs(got).max()
+
+
+@pytest.mark.parametrize("fused", [True, False])
+def test_barrier_engine_api_vs_reference(cuda, golden, fused):
+    """The drop-in engine builds the reference's barrier mesh from the option
+    (exponential_space(0, K, 170, 1/3) spots, v_max 10) and prices it through
+    the fused engine or the per-operator path."""
+    from fd_adi_gb300 import HestonFiniteDifferenceEngine
+    g = golden("barrier")
+    F = HestonFiniteDifferenceEngine(_barrier_option(), nspots=150, nvols=80, fused=fused)
+    # the fixture's meshes come from the reference on an x86-64 host; the C
+    # library's pow may round the last bit differently on other hosts
+    np.testing.assert_allclose(F.spots, g["S"], rtol=1e-14, atol=0)
+    np.testing.assert_allclose(F.vars, g["v"], rtol=1e-14, atol=0)
+    V0 = g["V0"]
+    for scheme, run in (("hv", lambda: F.solve_hundsdorferverwer(150, 1.0 / 150, V0, theta=0.5)),
+                        ("douglas", lambda: F.solve_douglas(150, 1.0 / 150, V0, theta=0.5)),
+                        ("smooth", lambda: F.solve_smooth(150, 1.0 / 150, V0))):
+        got = run()
+        assert _rel(got, g[scheme]) < 1e-11, scheme
+        assert abs(got[F.idx] - g[scheme][F.idx]) <= 1e-10 * abs(g[scheme][F.idx]), scheme
 
 
 @pytest.mark.parametrize("scheme", ["douglas", "hv", "implicit", "smooth", "cs", "mcs"])

@@ -90,3 +90,44 @@ def test_blackscholes(golden):
     i = int(np.argmin(np.abs(g["S"] - 100.0)))
     exact = analytic.bs_call(100.0, K, r, var, 1.0)[0]
     assert abs(g["douglas"][i] - exact) <= 1e-3 * exact
+
+
+BARRIER_SCHED = {
+    "implicit": [("implicit", 600, 1.0 / 600, 1.0)],
+    "douglas": [("douglas", 150, 1.0 / 150, 0.5)],
+    "hv": [("hv", 150, 1.0 / 150, 0.5)],
+    "smooth": [("implicit", 4, 1.0 / 300, 1.0), ("hv", 148, 1.0 / 150, 0.6)],
+}
+
+
+@pytest.mark.parametrize("scheme", sorted(BARRIER_SCHED))
+def test_barrier_vs_reference(golden, scheme):
+    """Up-and-out call of the reference's barrier test (rho = 0.4, theta =
+    0.12, barrier 170, 150 x 80): the oracle with the barrier's Dirichlet-0
+    spot boundary against the reference engine's grids."""
+    g = golden("barrier")
+    ref = g[scheme]
+    got = O.heston_solve(g["S"], g["v"], *g["params"], g["V0"], BARRIER_SCHED[scheme],
+                         barrier=True)
+    assert np.abs(got - ref).max() <= 1e-11 * np.abs(ref).max()
+    i, j = g["idx"]
+    assert abs(got[i, j] - ref[i, j]) <= 1e-13 * abs(ref[i, j])
+    # the barrier row stays at the Dirichlet value
+    assert np.abs(got[-1]).max() <= 1e-12 * np.abs(got).max()
+
+
+def test_oracle_constant_rates_match_constant_run():
+    """The oracle's per-step rebuild with every step at the option's own r is
+    the constant-coefficient solve, bit for bit; a rising rate changes it."""
+    from fd_adi_gb300 import mesh
+    S, v = mesh.heston_meshes(100., 95., 0.05, 40, 20, 760., 5.)
+    V0 = np.maximum(S[:, None] - 95., 0) * np.ones((1, v.size))
+    sch = [("implicit", 2, 0.025, 1.0), ("hv", 9, 0.05, HV_THETA)]
+    p = (0.03, 2.0, 0.05, 0.6, -0.5)
+    a = O.heston_solve(S, v, *p, V0, sch)
+    b = O.heston_solve(S, v, *p, V0, sch, rates=np.full(11, 0.03))
+    np.testing.assert_array_equal(a, b)
+    c = O.heston_solve(S, v, *p, V0, sch, rates=np.linspace(0.01, 0.06, 11))
+    assert np.abs(c - a).max() > 1e-3
+    with pytest.raises(ValueError):
+        O.heston_solve(S, v, *p, V0, sch, rates=np.full(10, 0.03))
