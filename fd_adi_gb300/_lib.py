@@ -30,7 +30,8 @@ class Tri(ctypes.Structure):
                 ("sup", ctypes.c_void_p), ("mid", ctypes.c_void_p), ("sub", ctypes.c_void_p),
                 ("R", ctypes.c_void_p), ("low_dirichlet", ctypes.c_void_p),
                 ("high_dirichlet", ctypes.c_void_p), ("top_factors", ctypes.c_void_p),
-                ("bottom_factors", ctypes.c_void_p)]
+                ("bottom_factors", ctypes.c_void_p), ("sup2", ctypes.c_void_p),
+                ("sub2", ctypes.c_void_p)]
 
 
 class Mixed(ctypes.Structure):

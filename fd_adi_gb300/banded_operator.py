@@ -92,6 +92,9 @@ class BandedOperator(object):
         self._has_low = False
         self._has_high = False
         self.has_residual = True
+        # [2, N] second off-diagonals inside the lines (A[r, r+2], A[r, r-2]) of
+        # a spliced upwind scheme, or None; the corners stay in the fold slots
+        self.band2 = None
         # mixed storage
         self.coeff = None
         self.w0 = None
@@ -138,12 +141,15 @@ class BandedOperator(object):
     # -- C-ABI views --
     def _tri(self):
         d = self.diags
+        b2 = self.band2
         return _lib.Tri(self.operator_rows, self.blocks, self.axis, int(self.has_residual),
                         int(self._has_low), int(self._has_high),
                         FOLD_CODES[self.top_fold_status], FOLD_CODES[self.bottom_fold_status],
                         d[0].data_ptr(), d[1].data_ptr(), d[2].data_ptr(), self.R.data_ptr(),
                         self.low_dirichlet.data_ptr(), self.high_dirichlet.data_ptr(),
-                        self.top_factors.data_ptr(), self.bottom_factors.data_ptr())
+                        self.top_factors.data_ptr(), self.bottom_factors.data_ptr(),
+                        b2[0].data_ptr() if b2 is not None else None,
+                        b2[1].data_ptr() if b2 is not None else None)
 
     def _mixed(self):
         return _lib.Mixed(self.n0, self.n1, int(self.has_residual), 0, self.coeff.data_ptr(),
@@ -166,7 +172,7 @@ class BandedOperator(object):
         B.has_residual = self.has_residual
         B._has_low, B._has_high = self._has_low, self._has_high
         for name in ("diags", "R", "low_dirichlet", "high_dirichlet", "top_factors",
-                     "bottom_factors", "coeff", "w0", "w1"):
+                     "bottom_factors", "band2", "coeff", "w0", "w1"):
             t = getattr(self, name)
             setattr(B, name, None if t is None else t.clone())
         B.n0, B.n1 = self.n0, self.n1
@@ -210,6 +216,12 @@ class BandedOperator(object):
             bots = rows[4, L - 1::L].copy()
             bot = CAN_FOLD
         self.top_fold_status, self.bottom_fold_status = top, bot
+        # second off-diagonals inside the lines (a spliced upwind scheme)
+        inner2 = rows[[0, 4]].copy()
+        inner2[0, ::L] = 0.0
+        inner2[1, L - 1::L] = 0.0
+        self.band2 = _dev(inner2) if np.any(inner2) and not (top == FOLDED or bot == FOLDED) \
+            else None
         self.diags = _dev(rows[1:4])
         R = other.R if other.R is not None else np.zeros(N)
         self.has_residual = other.R is not None
@@ -250,14 +262,17 @@ class BandedOperator(object):
         bot = self.bottom_factors.cpu().numpy()
         offsets = [1, 0, -1]
         data = [d[0], d[1], d[2]]
-        if self.top_fold_status == CAN_FOLD:
-            r = np.zeros(N)
-            r[::L] = top
+        b2 = self.band2.cpu().numpy() if self.band2 is not None else None
+        if self.top_fold_status == CAN_FOLD or b2 is not None:
+            r = np.zeros(N) if b2 is None else b2[0].copy()
+            if self.top_fold_status == CAN_FOLD:
+                r[::L] = top
             offsets.insert(0, 2)
             data.insert(0, r)
-        if self.bottom_fold_status == CAN_FOLD:
-            r = np.zeros(N)
-            r[L - 1::L] = bot
+        if self.bottom_fold_status == CAN_FOLD or b2 is not None:
+            r = np.zeros(N) if b2 is None else b2[1].copy()
+            if self.bottom_fold_status == CAN_FOLD:
+                r[L - 1::L] = bot
             offsets.append(-2)
             data.append(r)
         dia = np.zeros((len(offsets), N))
@@ -321,6 +336,11 @@ class BandedOperator(object):
         _lib.call("fdadi_tri_fold", ctypes.byref(t), int(top), int(bottom), unfold, _stream())
         self.top_fold_status = FOLD_NAMES[t.top_fold_status]
         self.bottom_fold_status = FOLD_NAMES[t.bottom_fold_status]
+        # a folded operator is tridiagonal: the second off-diagonals inside the
+        # lines are dropped, as the reference's diagonalize drops them
+        # (BandedOperator.pyx:195-198)
+        if self.is_folded():
+            self.band2 = None
 
     def is_folded(self):
         return self.top_fold_status == FOLDED or self.bottom_fold_status == FOLDED
@@ -355,8 +375,9 @@ class BandedOperator(object):
                                       "csrsv solve is marked untrustworthy and unused).")
         U = V if overwrite else V.clone()
         n0, n1 = self._grid_shape(U)
-        if self._scratch is None or self._scratch.numel() != self.operator_rows:
-            self._scratch = torch.empty(self.operator_rows, dtype=torch.float64, device=U.device)
+        need = self.operator_rows * (3 if self.band2 is not None else 1)
+        if self._scratch is None or self._scratch.numel() != need:
+            self._scratch = torch.empty(need, dtype=torch.float64, device=U.device)
         t = self._tri()
         _lib.call("fdadi_tri_solve", ctypes.byref(t), _ptr(U), n0, n1, _ptr(self._scratch),
                   _stream())
@@ -444,6 +465,8 @@ class BandedOperator(object):
             raise NotImplementedError("No add to diagonalized operator.")
         if other.is_folded():
             raise NotImplementedError("No add diagonalized operator.")
+        if other.band2 is not None and self.band2 is None:
+            self.band2 = torch.zeros_like(other.band2)
         a, b = self._tri(), other._tri()
         _lib.call("fdadi_tri_add_operator", ctypes.byref(a), ctypes.byref(b), _stream())
         self.top_fold_status = FOLD_NAMES[a.top_fold_status]
@@ -540,17 +563,82 @@ def heston_line(v, derivative, axis, barrier):
     return sub, mid, sup, R, extra, low, high
 
 
-def for_vector(v, blocks, derivative, axis, barrier=False):
+def upwind_rows(x, scheme, at):
+    """Rows ``at`` and beyond of a first-derivative operator whose scheme
+    switches there (the rows splice_with takes from the second scheme,
+    BandedOperator.pyx:527-591): 'forward' (forwardcoeffs, BandedOperator.pyx:
+    917-967: rows 1..n-3 use points i, i+1, i+2, row n-2 the centred
+    stencil) or 'backward' (backwardcoeffs, :1020-1067: rows 2..n-2 use
+    points i-2, i-1, i, row 1 the centred stencil). Returns (sup2, sup, mid,
+    sub, sub2), length n each, zero outside the rows that scheme fills."""
+    x = np.asarray(x, dtype=float)
+    n = x.size
+    e2, e1, e0, f1, f2 = (np.zeros(n) for _ in range(5))
+    if scheme == "forward":
+        for i in range(max(at, 1), n - 2):
+            d1, d2 = x[i + 1] - x[i], x[i + 2] - x[i + 1]
+            e1[i] = (d1 + d2) / (d1 * d2)
+            e2[i] = -d1 / (d2 * (d1 + d2))
+            e0[i] = (-2 * d1 - d2) / (d1 * (d1 + d2))
+        if n - 2 >= at:
+            dl, dm = x[n - 1] - x[n - 2], x[n - 2] - x[n - 3]
+            e1[n - 2] = dm / (dl * (dm + dl))
+            e0[n - 2] = (-dm + dl) / (dm * dl)
+            f1[n - 2] = -dl / (dm * (dm + dl))
+    elif scheme == "backward":
+        for i in range(max(at, 2), n - 1):
+            dp, di = x[i - 1] - x[i - 2], x[i] - x[i - 1]
+            e0[i] = (dp + 2 * di) / (di * (dp + di))
+            f1[i] = (-dp - di) / (dp * di)
+            f2[i] = di / (dp * (dp + di))
+        if at <= 1:
+            d1, d2 = x[1] - x[0], x[2] - x[1]
+            xx = d1 + d2
+            e1[1] = d1 / (d2 * xx)
+            e0[1] = (-d1 + d2) / (d1 * d2)
+            f1[1] = -d2 / (d1 * xx)
+    else:
+        raise ValueError("Unknown scheme: %s" % scheme)
+    return e2, e1, e0, f1, f2
+
+
+def for_vector(v, blocks, derivative, axis, barrier=False, scheme=None, at=None):
     """Heston derivative operator along ``axis`` replicated over ``blocks``
     lines, as FiniteDifference.BandedOperatorGPU.for_vector builds it
     (BandedOperatorGPU.pyx:599-618): spot operators (axis 0) carry the
     Dirichlet row at S = 0 and a residual; the variance second derivative is
-    CAN_FOLD at v_max."""
+    CAN_FOLD at v_max.
+
+    scheme, at: a first derivative whose rows from ``at`` on use 'forward' or
+    'backward' differences (the up/down-winding schemes HestonFiniteDifference-
+    Engine splices in, heston.py:414-439, FiniteDifferenceEngine.pyx:267-289).
+    The operator then has a second off-diagonal inside its lines and can fold
+    at that end, as the reference's spliced operator does."""
     sub, mid, sup, R, extra, low, high = heston_line(v, derivative, axis, barrier)
+    band2 = None
+    if scheme is not None:
+        n = np.asarray(v).size
+        if derivative != 1:
+            raise NotImplementedError("only first derivatives switch schemes")
+        if not 0 <= int(at) < n - 1:
+            raise ValueError("Cannot splice beyond the end of the vector. %i >= %i"
+                             % (int(at), n - 1))
+        e2, e1, e0, f1, f2 = upwind_rows(v, scheme, int(at))
+        # rows at.. come from the upwind scheme; the boundary rows stay
+        rows = np.arange(n)
+        take = (rows >= int(at)) & (rows >= 1) & (rows <= n - 2)
+        sup = np.where(take, e1, sup)
+        mid = np.where(take, e0, mid)
+        sub = np.where(take, f1, sub)
+        band2 = np.vstack([np.where(take, e2, 0.0), np.where(take, f2, 0.0)])
+        band2[0, 0] = 0.0
+        band2[1, n - 1] = 0.0
     B = BandedOperator()
     B.axis, B.blocks, B.derivative, B.order = int(axis), int(blocks), int(derivative), 2
     B.deltas = None
     B.diags = _dev(np.vstack([np.tile(sup, blocks), np.tile(mid, blocks), np.tile(sub, blocks)]))
+    if band2 is not None:
+        B.band2 = _dev(np.tile(band2, (1, blocks)))
     B.R = _dev(np.tile(R, blocks))
     B.has_residual = axis == 0
     B._has_low, B._has_high = low, high
@@ -558,8 +646,9 @@ def for_vector(v, blocks, derivative, axis, barrier=False):
     B.high_dirichlet = _dev(np.zeros(blocks))
     B.top_factors = _dev(np.zeros(blocks))
     B.bottom_factors = _dev(np.full(blocks, extra))
-    B.top_fold_status = CANNOT_FOLD
-    B.bottom_fold_status = CAN_FOLD if (axis == 1 and derivative == 2) else CANNOT_FOLD
+    B.top_fold_status = CAN_FOLD if scheme == "forward" else CANNOT_FOLD
+    B.bottom_fold_status = CAN_FOLD if ((axis == 1 and derivative == 2) or scheme == "backward") \
+        else CANNOT_FOLD
     return B
 
 

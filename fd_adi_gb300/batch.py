@@ -234,14 +234,69 @@ class HestonBatch(object):
 
         spot, variance: scalars or [n]; strikes, dt: [n]; params: [n, 5] of
         (r, kappa, theta, sigma, rho). V: the device state arena to use
-        (allocated on first use). Returns a numpy array of n prices (a view
-        of this batch's pinned buffer: copy it to keep it past the next call)."""
+        (allocated on first use). Returns a numpy array of n prices."""
+        mesh_kw = dict(spot_max_factor=spot_max_factor, var_max=var_max,
+                       spotdensity=spotdensity, varexp=varexp, threads=threads)
+        slot = self._stage(0, spot, strikes, variance, params, dt, **mesh_kw)
+        self._launch(slot, V, put)
+        return self._finish(slot)
+
+    def price_calls_many(self, sets, V=None, put=False, spot_max_factor=8.0, var_max=5.0,
+                         spotdensity=7.0, varexp=4.0, threads=0):
+        """price_calls over a sequence of option sets (each a tuple (spot,
+        strikes, variance, params, dt) on this batch's grid sizes), pipelined:
+        the host builds set k+1's meshes and indices into a second pinned
+        staging area while the device prices set k, so the host's share of a
+        set costs no device time. Returns a list of price arrays, in order."""
+        mesh_kw = dict(spot_max_factor=spot_max_factor, var_max=var_max,
+                       spotdensity=spotdensity, varexp=varexp, threads=threads)
+        out = []
+        it = iter(sets)
+        first = next(it, None)
+        if first is None:
+            return out
+        cur = self._stage(0, *first, **mesh_kw)
+        k = 1
+        for nxt in it:
+            self._launch(cur, V, put)
+            # set k's host work runs while the device prices set k - 1; the
+            # other slot's copies finished when its set was read back
+            staged = self._stage(k % 2, *nxt, **mesh_kw)
+            out.append(self._finish(cur))
+            cur = staged
+            k += 1
+        self._launch(cur, V, put)
+        out.append(self._finish(cur))
+        return out
+
+    def _slot(self, i):
+        """Pinned host staging area i (two, for price_calls_many)."""
+        if not hasattr(self, "_h"):
+            n = self.n
+            pin = lambda t: t.pin_memory()
+            self._h = [dict(spots=pin(torch.empty(self.spots.numel(), dtype=torch.float64)),
+                            vars=pin(torch.empty(self.vars.numel(), dtype=torch.float64)),
+                            params=pin(torch.empty(n * 5, dtype=torch.float64)),
+                            dt=pin(torch.empty(n, dtype=torch.float64)),
+                            K=pin(torch.empty(n, dtype=torch.float64)),
+                            idx=pin(torch.empty(n, dtype=torch.int64)),
+                            prices=pin(torch.empty(n, dtype=torch.float64)))
+                       for _ in range(2)]
+            self._d = dict(K=torch.empty(n, dtype=torch.float64, device=self.device),
+                           idx=torch.empty(n, dtype=torch.int64, device=self.device),
+                           prices=torch.empty(n, dtype=torch.float64, device=self.device))
+        return self._h[i]
+
+    def _stage(self, i, spot, strikes, variance, params, dt, spot_max_factor=8.0, var_max=5.0,
+               spotdensity=7.0, varexp=4.0, threads=0):
+        """Host part of price_calls into staging area i: meshes, price indices
+        and the per-option inputs."""
         n = self.n
         strikes = np.ascontiguousarray(strikes, dtype=np.float64).reshape(-1)
-        params = np.ascontiguousarray(params, dtype=np.float64).reshape(n, 5)
-        dt = np.broadcast_to(np.asarray(dt, dtype=np.float64), (n,))
         if strikes.size != n:
             raise ValueError("need %d strikes, got %d" % (n, strikes.size))
+        params = np.ascontiguousarray(params, dtype=np.float64).reshape(n, 5)
+        dt = np.broadcast_to(np.asarray(dt, dtype=np.float64), (n,))
         spot = np.broadcast_to(np.asarray(spot, dtype=np.float64), (n,))
         variance = np.broadcast_to(np.asarray(variance, dtype=np.float64), (n,))
         spots, vars_ = _mesh.heston_meshes_batch(spot, strikes, variance, self.n0, self.n1,
@@ -249,31 +304,24 @@ class HestonBatch(object):
                                                  spotdensity, varexp, threads=threads)
         flat = self.p_off[:-1] + _mesh.price_index_batch(spots, vars_, self.n0, self.n1, spot,
                                                          variance)
-        if not hasattr(self, "_h"):
-            pin = lambda t: t.pin_memory()
-            self._h = dict(spots=pin(torch.empty(self.spots.numel(), dtype=torch.float64)),
-                           vars=pin(torch.empty(self.vars.numel(), dtype=torch.float64)),
-                           params=pin(torch.empty(n * 5, dtype=torch.float64)),
-                           dt=pin(torch.empty(n, dtype=torch.float64)),
-                           K=pin(torch.empty(n, dtype=torch.float64)),
-                           idx=pin(torch.empty(n, dtype=torch.int64)),
-                           prices=pin(torch.empty(n, dtype=torch.float64)))
-            self._d = dict(K=torch.empty(n, dtype=torch.float64, device=self.device),
-                           idx=torch.empty(n, dtype=torch.int64, device=self.device),
-                           prices=torch.empty(n, dtype=torch.float64, device=self.device))
-        h, d = self._h, self._d
-        # the previous call's copies have completed (it synchronized)
+        h = self._slot(i)
         h["spots"].numpy()[:] = spots
         h["vars"].numpy()[:] = vars_
         h["params"].numpy()[:] = params.reshape(-1)
         h["dt"].numpy()[:] = dt
         h["K"].numpy()[:] = strikes
         h["idx"].numpy()[:] = flat
+        return h
+
+    def _launch(self, h, V=None, put=False):
+        """Device part of price_calls from a staging area, queued on the
+        batch's stream (the operator build waits for its own copies)."""
         if V is None:
             if getattr(self, "_V", None) is None:
                 self._V = torch.empty(self.total_points, dtype=torch.float64, device=self.device)
             V = self._V
         self._check_state(V)
+        d = self._d
         with torch.cuda.stream(self.stream):
             self.stream.wait_stream(torch.cuda.current_stream(self.device))
             self.spots.copy_(h["spots"], non_blocking=True)
@@ -287,12 +335,15 @@ class HestonBatch(object):
             self.run(V)
             self.gather(V, d["idx"], d["prices"])
             h["prices"].copy_(d["prices"], non_blocking=True)
+        self._last = h
+
+    def _finish(self, h):
         self.stream.synchronize()
-        return h["prices"].numpy()
+        return h["prices"].numpy().copy()
 
     def price_calls_last(self):
         """The prices of the last price_calls() (a copy)."""
-        return self._h["prices"].numpy().copy()
+        return self._last["prices"].numpy().copy()
 
     @property
     def price_calls_h2d_bytes(self):

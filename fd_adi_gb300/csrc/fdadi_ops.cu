@@ -60,16 +60,20 @@ __global__ void tri_apply_kernel(fdadi_tri_t op, const double *__restrict__ x, d
             if (k == L - 1 && highd) return op.high_dirichlet[b];
             return x[at(k)];
         };
-        double xm1 = 0.0, x0 = xin(0), x1 = xin(1);
+        double xm2 = 0.0, xm1 = 0.0, x0 = xin(0), x1 = xin(1);
         const double x2 = L > 2 ? xin(2) : 0.0;
         const double x_l3 = L > 2 ? xin(L - 3) : 0.0;
+        double xp2 = x2;   // x[k + 2]
+        const bool band = op.sup2 != nullptr;
         double yprev = 0.0, y0 = 0.0;
         for (int64_t k = 0; k < L; ++k) {
             const int64_t r = r0 + k;
             double acc = 0.0;
+            if (band && k >= 1 && k + 2 < L) acc += op.sup2[r] * xp2;
             if (k + 1 < L) acc += op.sup[r] * x1;
             acc += op.mid[r] * x0;
             if (k >= 1) acc += op.sub[r] * xm1;
+            if (band && k >= 2 && k < L - 1) acc += op.sub2[r] * xm2;
             if (k == 0 && op.top_fold_status == FDADI_CAN_FOLD) acc += op.top_factors[b] * x2;
             if (k == L - 1 && op.bottom_fold_status == FDADI_CAN_FOLD)
                 acc += op.bottom_factors[b] * x_l3;
@@ -94,9 +98,11 @@ __global__ void tri_apply_kernel(fdadi_tri_t op, const double *__restrict__ x, d
                 if (op.has_residual) yk += op.R[r];
                 y[at(k)] = yk;
             }
+            xm2 = xm1;
             xm1 = x0;
             x0 = x1;
             if (k + 2 < L) x1 = xin(k + 2);
+            if (band && k + 3 < L) xp2 = xin(k + 3);
         }
     }
 }
@@ -171,6 +177,82 @@ __global__ void tri_solve_kernel(fdadi_tri_t op, double *x, int64_t n1, double *
     }
 }
 
+// Banded solve of one line per thread: rows (A[k,k-2] .. A[k,k+2]), the
+// corner entries from the CAN_FOLD slots, eliminated top to bottom without row
+// exchanges, each row update rounded as written (no fused multiply-add), in
+// the order of a plain band elimination. The factored upper band (u0, u1, u2)
+// goes to scratch [3N], the forward-eliminated right-hand side to x; then back
+// substitution.
+struct BandRow {
+    double b2, b1, a0, a1, a2, r;
+};
+
+__global__ void band_solve_kernel(fdadi_tri_t op, double *x, int64_t n1, double *scratch) {
+    const int64_t N = op.operator_rows, L = op.operator_rows / op.blocks;
+    double *U0 = scratch, *U1 = scratch + N, *U2 = scratch + 2 * N;
+    for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < op.blocks;
+         b += (int64_t)gridDim.x * blockDim.x) {
+        LineMap at(op.axis, b, n1);
+        const int64_t r0 = b * L;
+        const bool lowd = op.has_low_dirichlet, highd = op.has_high_dirichlet;
+        auto row = [&](int64_t k) -> BandRow {
+            BandRow w{0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+            if (k >= L) return w;
+            const int64_t r = r0 + k;
+            double v;
+            if (k == 0 && lowd) v = op.low_dirichlet[b];
+            else if (k == L - 1 && highd) v = op.high_dirichlet[b];
+            else v = x[at(k)];
+            if (op.has_residual) v = v - op.R[r];
+            w.r = v;
+            w.a0 = op.mid[r];
+            if (k + 1 < L) w.a1 = op.sup[r];
+            if (k >= 1) w.b1 = op.sub[r];
+            if (k + 2 < L)
+                w.a2 = k == 0 ? (op.top_fold_status == FDADI_CAN_FOLD ? op.top_factors[b] : 0.0)
+                              : op.sup2[r];
+            if (k >= 2)
+                w.b2 = k == L - 1
+                           ? (op.bottom_fold_status == FDADI_CAN_FOLD ? op.bottom_factors[b] : 0.0)
+                           : op.sub2[r];
+            return w;
+        };
+        BandRow c0 = row(0), c1 = row(1), c2 = row(2);
+        for (int64_t k = 0; k < L; ++k) {
+            const double p = c0.a0;
+            if (k + 1 < L) {
+                const double l = __ddiv_rn(c1.b1, p);
+                c1.a0 = __dsub_rn(c1.a0, __dmul_rn(l, c0.a1));
+                c1.a1 = __dsub_rn(c1.a1, __dmul_rn(l, c0.a2));
+                c1.r = __dsub_rn(c1.r, __dmul_rn(l, c0.r));
+            }
+            if (k + 2 < L) {
+                const double l = __ddiv_rn(c2.b2, p);
+                c2.b1 = __dsub_rn(c2.b1, __dmul_rn(l, c0.a1));
+                c2.a0 = __dsub_rn(c2.a0, __dmul_rn(l, c0.a2));
+                c2.r = __dsub_rn(c2.r, __dmul_rn(l, c0.r));
+            }
+            const int64_t r = r0 + k;
+            U0[r] = c0.a0; U1[r] = c0.a1; U2[r] = c0.a2;
+            x[at(k)] = c0.r;
+            c0 = c1;
+            c1 = c2;
+            c2 = row(k + 3);
+        }
+        double xk1 = 0.0, xk2 = 0.0;
+        for (int64_t k = L - 1; k >= 0; --k) {
+            const int64_t r = r0 + k;
+            double acc = x[at(k)];
+            if (k + 1 < L) acc = __dsub_rn(acc, __dmul_rn(U1[r], xk1));
+            if (k + 2 < L) acc = __dsub_rn(acc, __dmul_rn(U2[r], xk2));
+            const double xk = __ddiv_rn(acc, U0[r]);
+            x[at(k)] = xk;
+            xk2 = xk1;
+            xk1 = xk;
+        }
+    }
+}
+
 __global__ void tri_scale_kernel(fdadi_tri_t op, const double *__restrict__ vec, double scalar) {
     const int64_t N = op.operator_rows, L = op.operator_rows / op.blocks;
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < N;
@@ -182,6 +264,7 @@ __global__ void tri_scale_kernel(fdadi_tri_t op, const double *__restrict__ vec,
         op.mid[r] *= v;
         op.sub[r] *= v;
         op.R[r] *= v;
+        if (op.sup2) { op.sup2[r] *= v; op.sub2[r] *= v; }
         if (k == 0 && op.top_fold_status == FDADI_CAN_FOLD) op.top_factors[b] *= v;
         if (k == L - 1 && op.bottom_fold_status == FDADI_CAN_FOLD) op.bottom_factors[b] *= v;
     }
@@ -204,6 +287,7 @@ __global__ void tri_add_operator_kernel(fdadi_tri_t a, fdadi_tri_t o) {
         const int64_t k = r % L, b = r / L;
         a.sup[r] += o.sup[r];
         a.sub[r] += o.sub[r];
+        if (o.sup2) { a.sup2[r] += o.sup2[r]; a.sub2[r] += o.sub2[r]; }
         if (!((k == 0 && a.has_low_dirichlet) || (k == L - 1 && a.has_high_dirichlet)))
             a.mid[r] += o.mid[r];
         a.R[r] += o.R[r];
@@ -302,6 +386,11 @@ static int check_tri(const fdadi_tri_t *op, int64_t n0, int64_t n1, bool grid) {
     FDADI_REQUIRE(op->sup && op->mid && op->sub && op->R && op->low_dirichlet &&
                       op->high_dirichlet && op->top_factors && op->bottom_factors,
                   "operator has a null array");
+    FDADI_REQUIRE((op->sup2 == nullptr) == (op->sub2 == nullptr),
+                  "sup2 and sub2 must both be set or both be NULL");
+    FDADI_REQUIRE(!op->sup2 || (op->top_fold_status != FDADI_FOLDED &&
+                                op->bottom_fold_status != FDADI_FOLDED),
+                  "a folded operator has no second off-diagonals (diagonalize drops them)");
     if (grid) {
         FDADI_REQUIRE(n0 > 0 && n1 > 0 && n0 * n1 == op->operator_rows,
                       "Dimension mismatch: grid %lld x %lld vs %lld operator rows",
@@ -348,8 +437,12 @@ int fdadi_tri_solve(const fdadi_tri_t *op, double *x, int64_t n0, int64_t n1, do
     if (rc) return rc;
     FDADI_REQUIRE(x && scratch, "null grid or scratch pointer");
     const int threads = 128;
-    tri_solve_kernel<<<grid_for(op->blocks, threads), threads, 0, as_stream(stream)>>>(*op, x, n1,
-                                                                                      scratch);
+    if (op->sup2)
+        band_solve_kernel<<<grid_for(op->blocks, threads), threads, 0, as_stream(stream)>>>(
+            *op, x, n1, scratch);
+    else
+        tri_solve_kernel<<<grid_for(op->blocks, threads), threads, 0, as_stream(stream)>>>(
+            *op, x, n1, scratch);
     FDADI_CHECK_LAUNCH();
     return FDADI_OK;
 }
@@ -388,6 +481,8 @@ int fdadi_tri_add_operator(fdadi_tri_t *self, const fdadi_tri_t *other, void *st
                   other->axis);
     FDADI_REQUIRE(self->operator_rows == other->operator_rows && self->blocks == other->blocks,
                   "Both operators must have the same length");
+    FDADI_REQUIRE(!other->sup2 || self->sup2,
+                  "add_operator: the operator added to must carry second off-diagonals too");
     if (self->top_fold_status == FDADI_FOLDED || self->bottom_fold_status == FDADI_FOLDED ||
         other->top_fold_status == FDADI_FOLDED || other->bottom_fold_status == FDADI_FOLDED) {
         set_error("Cannot add diagonalized operators.");
@@ -491,6 +586,8 @@ extern "C" int fdadi_tri_solve_noalloc(const fdadi_tri_t *op, double *x, int64_t
     int rc = check_tri(op, n0, n1, true);
     if (rc) return rc;
     FDADI_REQUIRE(x, "null grid pointer");
+    FDADI_REQUIRE(!op->sup2, "fdadi_tri_solve_noalloc: tridiagonal operators only (this one has "
+                             "second off-diagonals); use fdadi_tri_solve");
     FDADI_REQUIRE(op->operator_rows <= FDADI_NOALLOC_MAX_ROWS,
                   "fdadi_tri_solve_noalloc: %lld operator rows exceed the library scratch of %d "
                   "rows; use fdadi_tri_solve with caller scratch",

@@ -296,7 +296,10 @@ class FiniteDifferenceEngineADI(FiniteDifferenceEngine):
             cross = self.operators.get((0, 1))
             cross = cross.mul_scalar_from_host(dt) if cross is not None else None
             for L in Lis:
-                if L.is_foldable():
+                # folding the corner rows is the same system; an operator with
+                # second off-diagonals inside its lines (a switched scheme) is
+                # solved as a band, as the reference solves every implicit line
+                if L.is_foldable() and L.band2 is None:
                     L.diagonalize()
             return Lis, cross
 
@@ -391,8 +394,10 @@ class FiniteDifferenceEngineADI(FiniteDifferenceEngine):
         Lis = [o.mul_scalar_from_host(theta * -dt).add(1, inplace=True) for d, o in dims]
         for L in Les + Lis:
             L.enable_residual(False)
+        # the reference's Craig-Sneyd keeps full bandwidth; folding the corner
+        # rows is the same operator, a switched scheme's inner band is not
         for L in Les + Lis + Firsts:
-            if L.is_foldable():
+            if L.is_foldable() and L.band2 is None:
                 L.diagonalize()
         cross = self.operators.get((0, 1))
         c = theta * dt if modified else 0.5 * dt
@@ -462,8 +467,9 @@ class HestonFiniteDifferenceEngine(FiniteDifferenceEngineADI):
                  coefficients=None, boundaries=None, cache=True, verbose=True,
                  force_bandwidth=None, fused=True):
         FiniteDifferenceEngineADI.__init__(self)
-        if schemes is not None or flip_idx_var or flip_idx_spot:
-            raise NotImplementedError("Only central differencing supported on GPU")
+        if schemes is not None:
+            raise NotImplementedError("Only central differencing (with the flip_idx_spot / "
+                                      "flip_idx_var switches) is supported on GPU")
         assert isinstance(option, Option)
         self.option = option
         self.fused = fused
@@ -498,6 +504,24 @@ class HestonFiniteDifferenceEngine(FiniteDifferenceEngineADI):
             K = option.strike
             grid = Grid([self.spots, self.vars], initializer=lambda *x: np.maximum(x[0] - K, 0))
         self.spots[np.argmin(np.abs(self.spots - option.spot))] = option.spot
+        # up/down-winding (heston.py:414-439): forward differences in S from the
+        # strike on, backward differences in v from the mean variance on
+        from bisect import bisect_left
+        if flip_idx_var is True:
+            flip_idx_var = bisect_left(list(np.round(self.vars, decimals=5)),
+                                       np.round(option.variance.mean, decimals=5))
+        if flip_idx_spot is True:
+            flip_idx_spot = bisect_left(list(np.round(self.spots, decimals=5)),
+                                        np.round(option.strike, decimals=5))
+        self.flip_idx_spot = None if flip_idx_spot is False or flip_idx_spot is None \
+            else int(flip_idx_spot)
+        self.flip_idx_var = None if flip_idx_var is False or flip_idx_var is None \
+            else int(flip_idx_var)
+        if self.flip_idx_spot is not None or self.flip_idx_var is not None:
+            # the fused engine builds centred stencils only; the switched
+            # schemes run on the per-operator kernels (the reference GPU engine
+            # does not run them at all, FiniteDifferenceEngineGPU.pyx:634)
+            self.fused = False
         grid._mesh = (self.spots, self.vars)
         self.grid = grid
         self.gpugrid = _dev(self.grid.domain[-1])
@@ -508,9 +532,12 @@ class HestonFiniteDifferenceEngine(FiniteDifferenceEngineADI):
         """Single-derivative Heston operators (FiniteDifferenceEngineGPU.pyx:697-724)."""
         m0, m1 = self.spots, self.vars
         bar = bool(self.barrier)
-        self.simple_operators[(0,)] = for_vector(m0, m1.size, 1, 0, bar)
+        fs, fv = getattr(self, "flip_idx_spot", None), getattr(self, "flip_idx_var", None)
+        self.simple_operators[(0,)] = for_vector(m0, m1.size, 1, 0, bar,
+                                                 "forward" if fs is not None else None, fs)
         self.simple_operators[(0, 0)] = for_vector(m0, m1.size, 2, 0, bar)
-        self.simple_operators[(1,)] = for_vector(m1, m0.size, 1, 1, bar)
+        self.simple_operators[(1,)] = for_vector(m1, m0.size, 1, 1, bar,
+                                                 "backward" if fv is not None else None, fv)
         self.simple_operators[(1, 1)] = for_vector(m1, m0.size, 2, 1, bar)
         if getattr(self.option, "correlation", 0) != 0:
             self.simple_operators[(0, 1)] = mixed_for_vector(m0, m1)

@@ -98,6 +98,13 @@ typedef struct fdadi_tri {
     double *high_dirichlet;       /* [blocks] values forced on the last row */
     double *top_factors;          /* [blocks] CAN_FOLD: A[0,2]; FOLDED: fold factor */
     double *bottom_factors;       /* [blocks] CAN_FOLD: A[L-1,L-3]; FOLDED: fold factor */
+    double *sup2, *sub2;          /* [N] A[r, r+2] and A[r, r-2] inside the lines, or NULL:
+                                   * the rows a spliced upwind scheme gives a second
+                                   * off-diagonal (splice_with, BandedOperator.pyx:527-591).
+                                   * The corner entries A[0,2], A[L-1,L-3] stay in the fold
+                                   * slots (sup2[row 0], sub2[row L-1] unused). Not allowed on
+                                   * a FOLDED operator: diagonalize drops them, as the
+                                   * reference's does (BandedOperator.pyx:181-198). */
 } fdadi_tri_t;
 
 /* y = A x (+ R if has_residual), x with its Dirichlet entries forced first;
@@ -108,7 +115,10 @@ int fdadi_tri_apply(const fdadi_tri_t *op, const double *x, double *y,
 
 /* x <- A^-1 (x_forced - R): Dirichlet entries forced, residual subtracted if
  * enabled, right-hand side folded, then one Thomas solve per line. A CAN_FOLD
- * operator is folded on the fly (same linear system). scratch: [N] doubles.
+ * operator is folded on the fly (same linear system). With sup2/sub2 the line
+ * is solved as a band of width 2 + 2 by LU without row exchanges (the system
+ * scipy's solve_banded solves in the reference CPU engine, BandedOperator.pyx:
+ * 364-394). scratch: [N] doubles, [3N] with sup2/sub2.
  * Replaces _TriBandedOperator::solve (_TriBandedOperatorGPU.cu:719-770). */
 int fdadi_tri_solve(const fdadi_tri_t *op, double *x, int64_t n0, int64_t n1,
                     double *scratch, void *stream);

@@ -157,9 +157,75 @@ static void boundary_line(op_t *B, int o0, const double *x, int n, int derivativ
     }
 }
 
+/* forwardcoeffs (BandedOperator.pyx:917-967), first derivative, order 2, for
+ * the rows a spliced 'forward' scheme takes (rows >= at): rows 1..n-3 use the
+ * 3-point forward stencil (i, i+1, i+2), row n-2 the centred one. Rows are
+ * written into the 5 diagonals at line offset o0 (offsets 2, 1, 0, -1, -2). */
+static void forward_rows(op_t *B, int o0, const double *x, int n, int at) {
+    double *e2 = B->d[0] + o0, *e1 = B->d[1] + o0, *e0 = B->d[2] + o0,
+           *f1 = B->d[3] + o0, *f2 = B->d[4] + o0;
+    for (int i = at; i < n; ++i) { e2[i] = e1[i] = e0[i] = f1[i] = f2[i] = 0; }
+    for (int i = at > 1 ? at : 1; i < n - 2; ++i) {
+        double d1 = x[i + 1] - x[i], d2 = x[i + 2] - x[i + 1];
+        e1[i] = (d1 + d2) / (d1 * d2);
+        e2[i] = -d1 / (d2 * (d1 + d2));
+        e0[i] = (-2 * d1 - d2) / (d1 * (d1 + d2));
+    }
+    if (n - 2 >= at) {
+        double dl = x[n - 1] - x[n - 2], dm = x[n - 2] - x[n - 3];
+        e1[n - 2] = dm / (dl * (dm + dl));
+        e0[n - 2] = (-dm + dl) / (dm * dl);
+        f1[n - 2] = -dl / (dm * (dm + dl));
+    }
+}
+
+/* backwardcoeffs (BandedOperator.pyx:1020-1067), first derivative, order 2,
+ * for rows >= at: rows 2..n-2 use the 3-point backward stencil (i-2, i-1, i),
+ * row 1 the centred one. */
+static void backward_rows(op_t *B, int o0, const double *x, int n, int at) {
+    double *e2 = B->d[0] + o0, *e1 = B->d[1] + o0, *e0 = B->d[2] + o0,
+           *f1 = B->d[3] + o0, *f2 = B->d[4] + o0;
+    for (int i = at; i < n; ++i) { e2[i] = e1[i] = e0[i] = f1[i] = f2[i] = 0; }
+    for (int i = at > 2 ? at : 2; i < n - 1; ++i) {
+        double dp = x[i - 1] - x[i - 2], di = x[i] - x[i - 1];
+        e0[i] = (dp + 2 * di) / (di * (dp + di));
+        f1[i] = (-dp - di) / (dp * di);
+        f2[i] = di / (dp * (dp + di));
+    }
+    if (at <= 1) {
+        double d1 = x[1] - x[0], d2 = x[2] - x[1];
+        double xx = d1 + d2;
+        e1[1] = d1 / (d2 * xx);
+        e0[1] = (-d1 + d2) / (d1 * d2);
+        f1[1] = -d2 / (d1 * xx);
+    }
+}
+
 /* for_vector + applyboundary + _replicate/_flatten_tensor_aligned
  * (FiniteDifferenceEngine.pyx:446-497): one derivative operator along `axis`
- * replicated over `blocks` lines, same boundary on every line. */
+ * replicated over `blocks` lines, same boundary on every line. `splice`: 0
+ * none, 1 a 'forward' scheme from row `at` on, 2 a 'backward' scheme from row
+ * `at` on (first derivatives; make_operator_template and splice_with,
+ * FiniteDifferenceEngine.pyx:267-289, BandedOperator.pyx:527-591: every row
+ * >= at comes from the second scheme's operator). */
+static op_t *derivative_op_spliced(const double *x, int n, int blocks, int axis, int derivative,
+                                   int ltype, double lval, int htype, double hval, int pentadiag,
+                                   int splice, int at) {
+    op_t *B = op_new(blocks, n, axis);
+    for (int b = 0; b < blocks; ++b) {
+        int o0 = b * n;
+        center_line(x, n, derivative, B->d[1] + o0, B->d[2] + o0, B->d[3] + o0);
+        if (splice == 1) forward_rows(B, o0, x, n, at);
+        else if (splice == 2) backward_rows(B, o0, x, n, at);
+        boundary_line(B, o0, x, n, derivative, ltype, lval, htype, hval, b);
+    }
+    /* the operator's offsets include +2 (forward) or -2 (backward), so it can
+     * fold there (BandedOperator.pyx:64-65) */
+    B->bot_status = (pentadiag || splice == 2) ? CAN_FOLD : CANNOT_FOLD;
+    B->top_status = splice == 1 ? CAN_FOLD : CANNOT_FOLD;
+    return B;
+}
+
 static op_t *derivative_op(const double *x, int n, int blocks, int axis, int derivative,
                            int ltype, double lval, int htype, double hval, int pentadiag) {
     op_t *B = op_new(blocks, n, axis);
@@ -370,6 +436,66 @@ static void op_apply(const op_t *o, const double *V, int n0, int n1, double *out
  * RHS folded, then a tridiagonal solve per line. Operators that still carry a
  * +-2 diagonal (the unfolded implicit operator) are folded on a private copy
  * first, which is the same linear system. */
+/* True if the +2 (-2) diagonal holds entries beyond the first (last) row of a
+ * line: a spliced forward (backward) scheme, which folding cannot remove. */
+static int op_interior_band(const op_t *o) {
+    for (int b = 0; b < o->blocks; ++b)
+        for (int k = 0; k < o->L; ++k) {
+            int i = b * o->L + k;
+            if (k != 0 && o->d[0][i] != 0) return 1;
+            if (k != o->L - 1 && o->d[4][i] != 0) return 1;
+        }
+    return 0;
+}
+
+/* Banded LU without pivoting on every line (offsets 2..-2), the system
+ * scipy's solve_banded solves (LAPACK gbsv; no row exchange happens on these
+ * diagonally dominant systems, so they agree to rounding). x: right-hand
+ * sides in, solutions out, block-major. */
+static void band_solve(const op_t *o, double *x) {
+    int L = o->L;
+#pragma omp parallel if (o->N >= PAR_MIN)
+    {
+    double *a2 = (double *)malloc((size_t)L * sizeof(double));
+    double *a1 = (double *)malloc((size_t)L * sizeof(double));
+    double *a0 = (double *)malloc((size_t)L * sizeof(double));
+    double *b1 = (double *)malloc((size_t)L * sizeof(double));
+    double *b2 = (double *)malloc((size_t)L * sizeof(double));
+#pragma omp for
+    for (int b = 0; b < o->blocks; ++b) {
+        int r0 = b * L;
+        double *r = x + (size_t)r0;
+        memcpy(a2, o->d[0] + r0, (size_t)L * sizeof(double));
+        memcpy(a1, o->d[1] + r0, (size_t)L * sizeof(double));
+        memcpy(a0, o->d[2] + r0, (size_t)L * sizeof(double));
+        memcpy(b1, o->d[3] + r0, (size_t)L * sizeof(double));
+        memcpy(b2, o->d[4] + r0, (size_t)L * sizeof(double));
+        for (int k = 0; k < L; ++k) {
+            double p = a0[k];
+            if (k + 1 < L) {
+                double l = b1[k + 1] / p;
+                a0[k + 1] = a0[k + 1] - l * a1[k];
+                a1[k + 1] = a1[k + 1] - l * a2[k];
+                r[k + 1] = r[k + 1] - l * r[k];
+            }
+            if (k + 2 < L) {
+                double l = b2[k + 2] / p;
+                b1[k + 2] = b1[k + 2] - l * a1[k];
+                a0[k + 2] = a0[k + 2] - l * a2[k];
+                r[k + 2] = r[k + 2] - l * r[k];
+            }
+        }
+        for (int k = L - 1; k >= 0; --k) {
+            double acc = r[k];
+            if (k + 1 < L) acc = acc - a1[k] * r[k + 1];
+            if (k + 2 < L) acc = acc - a2[k] * r[k + 2];
+            r[k] = acc / a0[k];
+        }
+    }
+    free(a2); free(a1); free(a0); free(b1); free(b2);
+    }
+}
+
 static void op_solve(const op_t *o_in, double *V, int n0, int n1) {
     const op_t *o = o_in;
     op_t *tmp = NULL;
@@ -378,6 +504,12 @@ static void op_solve(const op_t *o_in, double *V, int n0, int n1) {
     gather(o, V, n0, n1, x);
     force_dirichlet(o, x);
     if (o->has_R) for (int i = 0; i < N; ++i) x[i] = x[i] - o->R[i];
+    if (!op_folded(o) && op_interior_band(o)) {
+        band_solve(o, x);
+        scatter(o, x, n0, n1, V);
+        free(x);
+        return;
+    }
     if (op_foldable(o)) {
         tmp = op_copy(o);
         op_diagonalize(tmp);
@@ -427,20 +559,23 @@ static void engine_free(engine_t *E) {
  * and (0,0) takes (0,)'s boundaries (heston.py:361-370). */
 static void heston_engine(engine_t *E, const double *S, int nS, const double *v, int nv,
                           double r, double kappa, double theta, double sigma, double rho,
-                          int barrier) {
+                          int barrier, int flip_spot, int flip_var) {
     int N = nS * nv;
     E->ndim = 2; E->n0 = nS; E->n1 = nv;
     double *vec = (double *)malloc((size_t)N * sizeof(double));
-    /* (0,): D U=0 / Neumann dU/dS = 1 (barrier: D U=0) */
-    op_t *d0 = barrier
-        ? derivative_op(S, nS, nv, 0, 1, BND_DIRICHLET, 0.0, BND_DIRICHLET, 0.0, 0)
-        : derivative_op(S, nS, nv, 0, 1, BND_DIRICHLET, 0.0, BND_NEUMANN, 1.0, 0);
+    /* (0,): D U=0 / Neumann dU/dS = 1 (barrier: D U=0); from flip_spot on
+     * (>= 0), forward differences (heston.py:432-433) */
+    op_t *d0 = derivative_op_spliced(S, nS, nv, 0, 1, BND_DIRICHLET, 0.0,
+                                     barrier ? BND_DIRICHLET : BND_NEUMANN, barrier ? 0.0 : 1.0,
+                                     0, flip_spot >= 0 ? 1 : 0, flip_spot);
     /* (0,0): D U=0 / free, first derivative 1 (barrier: D U=0) */
     op_t *d00 = barrier
         ? derivative_op(S, nS, nv, 0, 2, BND_DIRICHLET, 0.0, BND_DIRICHLET, 0.0, 0)
         : derivative_op(S, nS, nv, 0, 2, BND_DIRICHLET, 0.0, BND_NONE, 1.0, 0);
-    /* (1,): free / free */
-    op_t *d1 = derivative_op(v, nv, nS, 1, 1, BND_NONE, NAN, BND_NONE, NAN, 0);
+    /* (1,): free / free; from flip_var on (>= 0), backward differences
+     * (heston.py:436-437) */
+    op_t *d1 = derivative_op_spliced(v, nv, nS, 1, 1, BND_NONE, NAN, BND_NONE, NAN, 0,
+                                     flip_var >= 0 ? 2 : 0, flip_var);
     /* (1,1): Neumann 0 / free second order (offset -2) */
     op_t *d11 = derivative_op(v, nv, nS, 1, 2, BND_NEUMANN, 0.0, BND_NONE, NAN, 1);
 
@@ -655,11 +790,10 @@ static void run_cs(const engine_t *E, int n, double dt, double theta, double *V,
         op_add_scalar_f32(Li[d], 1.0);
         Le[d]->has_R = 0; Li[d]->has_R = 0;
     }
-    for (int d = 0; d < nd; ++d) {
-        if (op_foldable(Le[d])) op_diagonalize(Le[d]);
-        if (op_foldable(Li[d])) op_diagonalize(Li[d]);
-    }
-    for (int k = 0; k < nf; ++k) if (op_foldable(F[k]) && !F[k]->mixed) op_diagonalize(F[k]);
+    /* Craig-Sneyd keeps every operator at full bandwidth (the reference does
+     * not diagonalize here): applies use all five diagonals and solves the
+     * whole band, which matters once a spliced scheme puts +-2 entries inside
+     * the lines. */
     double *Y = (double *)malloc(N * sizeof(double)), *Y0 = (double *)malloc(N * sizeof(double)),
            *D = (double *)malloc(N * sizeof(double)), *T = (double *)malloc(N * sizeof(double));
     for (int s = 0; s < n; ++s) {
@@ -723,9 +857,13 @@ int oracle_heston_solve(const double *S, int nS, const double *v, int nv,
                         int nseg, const int *scheme, const int *nsteps,
                         const double *dt, const double *th, double *V, const double *rates) {
     if (nS < 4 || nv < 4) return 1;
+    /* flags bits 8..19: flip_idx_spot + 1, bits 20..30: flip_idx_var + 1 (0: none) */
+    const int flip_spot = ((flags >> 8) & 0xFFF) - 1, flip_var = ((flags >> 20) & 0x7FF) - 1;
+    if (flip_spot >= nS - 1 || flip_var >= nv - 1) return 1;
     engine_t E;
     if (!rates) {
-        heston_engine(&E, S, nS, v, nv, r, kappa, theta, sigma, rho, (flags & 2) != 0);
+        heston_engine(&E, S, nS, v, nv, r, kappa, theta, sigma, rho, (flags & 2) != 0,
+                      flip_spot, flip_var);
         if ((flags & 1) && rho == 0) { op_free(E.M); E.M = NULL; }
         run_schedule(&E, nseg, scheme, nsteps, dt, th, V);
         engine_free(&E);
@@ -738,7 +876,8 @@ int oracle_heston_solve(const double *S, int nS, const double *v, int nv,
     int k = 0;
     for (int sg = 0; sg < nseg; ++sg) {
         for (int s = 0; s < nsteps[sg]; ++s, ++k) {
-            heston_engine(&E, S, nS, v, nv, rates[k], kappa, theta, sigma, rho, (flags & 2) != 0);
+            heston_engine(&E, S, nS, v, nv, rates[k], kappa, theta, sigma, rho, (flags & 2) != 0,
+                          flip_spot, flip_var);
             if ((flags & 1) && rho == 0) { op_free(E.M); E.M = NULL; }
             const int one = 1;
             run_schedule(&E, 1, scheme + sg, &one, dt + sg, th + sg, V);
@@ -770,7 +909,7 @@ int oracle_heston_operators(const double *S, int nS, const double *v, int nv,
                             int *status) {
     if (nS < 4 || nv < 4) return 1;
     engine_t E;
-    heston_engine(&E, S, nS, v, nv, r, kappa, theta, sigma, rho, 0);
+    heston_engine(&E, S, nS, v, nv, r, kappa, theta, sigma, rho, 0, -1, -1);
     size_t N = (size_t)nS * nv;
     for (int k = 0; k < 5; ++k) {
         memcpy(A0 + k * N, E.A[0]->d[k], N * sizeof(double));

@@ -78,18 +78,29 @@ def _schedule(schedule):
     return sc, ns, dt, th
 
 
+def _flags(drop_zero_mixed, barrier, flip_spot, flip_var):
+    f = int(bool(drop_zero_mixed)) | (2 if barrier else 0)
+    if flip_spot is not None:
+        f |= (int(flip_spot) + 1) << 8
+    if flip_var is not None:
+        f |= (int(flip_var) + 1) << 20
+    return f
+
+
 def heston_solve(spots, vars_, r, kappa, theta, sigma, rho, V0, schedule, drop_zero_mixed=False,
-                 barrier=False, rates=None):
+                 barrier=False, rates=None, flip_spot=None, flip_var=None):
     """Run a schedule of ADI segments on the reference Heston operators
     (barrier: the top of the spot mesh is an up-and-out barrier; rates: the
-    interest rate of every step, the operators rebuilt before each)."""
+    interest rate of every step, the operators rebuilt before each;
+    flip_spot / flip_var: the row from which the spot first derivative uses
+    forward and the variance first derivative backward differences)."""
     S = np.ascontiguousarray(spots, dtype=np.float64)
     v = np.ascontiguousarray(vars_, dtype=np.float64)
     V = np.array(V0, dtype=np.float64, order="C").copy()
     assert V.shape == (S.size, v.size)
     sc, ns, dt, th = _schedule(schedule)
     rc = lib().oracle_heston_solve(_dp(S), S.size, _dp(v), v.size, r, kappa, theta, sigma, rho,
-                                   int(bool(drop_zero_mixed)) | (2 if barrier else 0),
+                                   _flags(drop_zero_mixed, barrier, flip_spot, flip_var),
                                    len(sc), _ip(sc), _ip(ns), _dp(dt),
                                    _dp(th), _dp(V), _rates(rates, int(ns.sum())))
     if rc:

@@ -60,10 +60,13 @@ def heston_mesh(S0, K, v0, nS, nv, spot_max, var_max, spotdensity=7.0, varexp=4.
     return spots, np.array(vars_, dtype=float)
 
 
-def heston_engine(S0, K, r, v0, kappa, theta, sigma, rho, spots, vars_, barrier=False):
+def heston_engine(S0, K, r, v0, kappa, theta, sigma, rho, spots, vars_, barrier=False,
+                  flip_spot=None, flip_var=None):
     """A reference FiniteDifferenceEngineADI with the Heston PDE (heston.py:302-359);
     barrier: an up-and-out barrier at the top of the spot mesh, whose spot
-    boundaries become Dirichlet 0 at both ends (heston.py:361-370)."""
+    boundaries become Dirichlet 0 at both ends (heston.py:361-370);
+    flip_spot / flip_var: spliced 'forward' / 'backward' first-derivative
+    schemes from that row on (heston.py:414-439)."""
     FD, BO, U, Grid = _import()
 
     def mu_s(t, *dim):
@@ -103,6 +106,10 @@ def heston_engine(S0, K, r, v0, kappa, theta, sigma, rho, spots, vars_, barrier=
         boundaries[(0,)] = (boundaries[(0,)][0], (0, lambda *x: 0.0))
         boundaries[(0, 0)] = boundaries[(0,)]
     schemes = {(0,): [{"scheme": "center"}], (1,): [{"scheme": "center"}]}
+    if flip_spot is not None:
+        schemes[(0,)].append({"scheme": "forward", "from": int(flip_spot)})
+    if flip_var is not None:
+        schemes[(1,)].append({"scheme": "backward", "from": int(flip_var)})
     grid = Grid([spots, vars_], initializer=lambda *x: np.maximum(x[0] - K, 0))
     F = FD.FiniteDifferenceEngineADI(grid, coefficients=coefficients,
                                      boundaries=boundaries, schemes=schemes)

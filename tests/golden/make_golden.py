@@ -217,6 +217,29 @@ def heston1024x512_nt1000(cached=None):
                         vmax=np.array(np.abs(V).max()))
 
 
+def upwind():
+    """Up/down-winding (heston.py:414-439): the spot first derivative switches
+    to forward differences from the strike's grid index on (flip_idx_spot),
+    the variance first derivative to backward differences from the mean
+    variance's (flip_idx_var); 40 x 24 grid, rho = -0.7, sigma = 0.5, both
+    switches alone and together, for the implicit, Douglas, HV, smooth,
+    Craig-Sneyd and modified Craig-Sneyd solves (20 steps of 0.01)."""
+    from bisect import bisect_left
+    S, v = H.heston_mesh(100., 100., 0.04, 40, 24, 800., 5.)
+    fs = bisect_left(list(np.round(S, decimals=5)), np.round(100., decimals=5))
+    fv = bisect_left(list(np.round(v, decimals=5)), np.round(0.04, decimals=5))
+    p = (0.06, 1.0, 0.04, 0.5, -0.7)
+    out = dict(S=S, v=v, params=np.array(p), flips=np.array([fs, fv]))
+    for tag, (a, b) in (("s", (fs, None)), ("v", (None, fv)), ("sv", (fs, fv))):
+        F = H.heston_engine(100., 100., p[0], 0.04, p[1], p[2], p[3], p[4], S, v,
+                            flip_spot=a, flip_var=b)
+        V0 = F.grid.domain[-1].copy()
+        out["V0"] = V0
+        for name, fn in SCHEDULES.items():
+            out["%s_%s" % (tag, name)] = fn(F, 20, 0.01, V0)[0]
+    np.savez_compressed(os.path.join(HERE, "upwind.npz"), **out)
+
+
 def blackscholes():
     """1-D Black-Scholes, the reference test case (tests/test_BlackScholesOption.py:24-75):
     S=100, K=99, r=0.06, var=0.04, T=1, 150 spots to 5000 with density 1."""
@@ -250,6 +273,7 @@ if __name__ == "__main__":
     heston1024x512_short()
     blackscholes()
     barrier()
+    upwind()
     heston1024x512_nt1000(os.environ.get("FDADI_CFG2_CACHE"))
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):

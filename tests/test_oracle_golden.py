@@ -131,3 +131,30 @@ def test_oracle_constant_rates_match_constant_run():
     assert np.abs(c - a).max() > 1e-3
     with pytest.raises(ValueError):
         O.heston_solve(S, v, *p, V0, sch, rates=np.full(10, 0.03))
+
+
+UPWIND_SCHED = {
+    "douglas": [("douglas", 20, 0.01, 0.5)],
+    "hv": [("hv", 20, 0.01, HV_THETA)],
+    "implicit": [("implicit", 20, 0.01, 1.0)],
+    "smooth": [("implicit", 2, 0.005, 1.0), ("hv", 19, 0.01, 0.6)],
+    "cs": [("cs", 20, 0.01, 0.5)],
+    "mcs": [("mcs", 20, 0.01, 1.0 / 3)],
+}
+
+
+@pytest.mark.parametrize("tag", ["s", "v", "sv"])
+@pytest.mark.parametrize("scheme", sorted(UPWIND_SCHED))
+def test_upwind_schemes_vs_reference(golden, tag, scheme):
+    """Switched first-derivative schemes (forward in S from the strike's
+    index, backward in v from the mean variance's) against the reference
+    engine: HV, Douglas and smooth on the diagonalized operators (whose inner
+    +-2 entries the reference drops), implicit and Craig-Sneyd on the full
+    band."""
+    g = golden("upwind")
+    fs, fv = (int(x) for x in g["flips"])
+    flips = {"s": (fs, None), "v": (None, fv), "sv": (fs, fv)}[tag]
+    got = O.heston_solve(g["S"], g["v"], *g["params"], g["V0"], UPWIND_SCHED[scheme],
+                         flip_spot=flips[0], flip_var=flips[1])
+    ref = g["%s_%s" % (tag, scheme)]
+    assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
