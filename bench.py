@@ -74,7 +74,7 @@ NCU_TRAFFIC_B_PER_POINT = {"explicit_hv0": 52.7, "explicit_hv3": 62.3, "spot_sol
 # busy with DFMA (2 flops each; DMUL and DADD occupy it the same) reads as the
 # DFMA peak that fdadi_fp64_probe measures. The mixed-term row sums are formed
 # for 18 staged rows per 16-row tile: 3 x 18/16 = 3.375 instructions per point.
-STAGE_FLOPS = {"explicit_hv0": 30.75, "explicit_hv3": 28.75, "spot_solve": 8, "var_solve_y2": 6,
+STAGE_FLOPS = {"explicit_hv0": 30.75, "explicit_hv3": 32.75, "spot_solve": 8, "var_solve_y2": 6,
                "var_solve_v": 6, "explicit_implicit": 12.75, "var_solve_implicit": 6,
                "spot_solve_implicit": 6}
 
@@ -640,8 +640,12 @@ def parity(batch, V, prices, sample):
         if g is not None:
             mine = Vh[batch.p_off[k]:batch.p_off[k + 1]].reshape(batch.n0[k], batch.n1[k])
             grel.append(float(np.abs(mine - g).max() / max(np.abs(g).max(), 1e-300)))
+    worst = sorted(range(len(idx)), key=lambda m: -prel[m])[:3]
     return {"n": len(idx), "max_price_rel": float(max(prel)),
             "max_grid_rel_on_sample": float(max(grel)) if grel else None,
+            "worst": [{"option": int(idx[m]), "nS": int(batch.n0[idx[m]]),
+                       "nv": int(batch.n1[idx[m]]), "price": float(ref_prices[m]),
+                       "price_rel": float(prel[m])} for m in worst],
             "price_bar": 1e-10, "grid_bar": 1e-9,
             "ok": bool(max(prel) <= 1e-10 and (not grel or max(grel) <= 1e-9))}
 

@@ -89,6 +89,12 @@ struct Arena {
     double *w0i, *RSi, *LSi, *LVvi, *foldVi, *LVzi;
     // HV corrector: (1/2 - theta) * F0 [3P] and w0 / 2 [3 SS]
     double *F0h, *w0h;
+    // HV corrector: the variance operator times theta dt rounded as the
+    // reference's Les are, (A1 * theta) * dt ([3 SV] rows on S > 0, its
+    // A[n1-1, n1-3], the S = 0 diagonal), and a per-option 1 (the corrector's
+    // spot solve subtracts that product as it stands)
+    double *LE1v, *LE1x, *LE1z, *one;
+    double *F1h;               // [3 SV] F1v / 2 (exact): the corrector's 1/2 F1 Y2 in its chain
     double *sw;                // [6 SS] spot stencil weights for the builders
     // stage buffers
     double *FV, *W, *T, *Y2;
@@ -324,6 +330,11 @@ __global__ void build_options_kernel(Arena A, BuildArgs a) {
     A.F1x[o] = MUL(xb.ext, dt);
     const Row3 z = var_row(v, n1, 0, 0.0, r, half_r, kappa, th, sigma);
     A.F1z[o] = MUL(z.mid, dt);
+    if (a.hv) {
+        A.LE1x[o] = MUL(MUL(xb.ext, a.theta), dt);
+        A.LE1z[o] = MUL(MUL(z.mid, a.theta), dt);
+        A.one[o] = 1.0;
+    }
     var_factors(A, o, v, n1, r, half_r, kappa, th, sigma, MUL(a.theta, -dt), A.LVv, A.foldV,
                 &A.LVz[o]);
     if (a.smoothing)
@@ -393,6 +404,14 @@ __global__ void build_points_kernel(Arena A, BuildArgs a) {
         const Row3 w = var_row(v, n1, j, 1.0, r, half_r, kappa, th, sigma);
         A.F1v[q] = MUL(w.sub, dt); A.F1v[A.SV + q] = MUL(w.mid, dt);
         A.F1v[2 * A.SV + q] = MUL(w.sup, dt);
+        if (a.hv) {
+            A.LE1v[q] = MUL(MUL(w.sub, a.theta), dt);
+            A.LE1v[A.SV + q] = MUL(MUL(w.mid, a.theta), dt);
+            A.LE1v[2 * A.SV + q] = MUL(MUL(w.sup, a.theta), dt);
+            A.F1h[q] = 0.5 * A.F1v[q];
+            A.F1h[A.SV + q] = 0.5 * A.F1v[A.SV + q];
+            A.F1h[2 * A.SV + q] = 0.5 * A.F1v[2 * A.SV + q];
+        }
     }
 }
 
@@ -548,16 +567,29 @@ __device__ __forceinline__ void explicit_tile(const Arena &A, const double *__re
             acc = fma(A.w0h[A.SS + so + i], sT[ty + 1][tx], acc);
             acc = fma(A.w0h[2 * A.SS + so + i], sT[ty + 2][tx], acc);
         }
-        double a1;
+        // 1/2 F1 Y2 joins the chain through the halved copy of F1 (an exact
+        // scaling); the corrector's variance term theta dt A1 Y2 is formed
+        // apart, with the reference's (A1 theta) dt coefficients: these
+        // operators are built once, so a coefficient rounded otherwise (theta
+        // times dt A1, or 1/2 F1 taken from it) would bias every step alike,
+        // and over a run the price drifts by up to ~1e-10
+        double le;
         if (i == 0 && (fl & OPT_ROW0_ZERO)) {
-            a1 = A.F1z[o] * xc;
+            acc = fma(0.5 * A.F1z[o], xc, acc);
+            le = A.LE1z[o] * xc;
         } else {
-            a1 = A.F1v[js] * sX[ty + 1][tx + 1] + A.F1v[A.SV + js] * xc +
-                 A.F1v[2 * A.SV + js] * sX[ty + 1][tx + 3];
-            if (j == n1 - 1) a1 += A.F1x[o] * sX[ty + 1][tx];
+            acc = fma(A.F1h[js], sX[ty + 1][tx + 1], acc);
+            acc = fma(A.F1h[A.SV + js], xc, acc);
+            acc = fma(A.F1h[2 * A.SV + js], sX[ty + 1][tx + 3], acc);
+            le = A.LE1v[js] * sX[ty + 1][tx + 1] + A.LE1v[A.SV + js] * xc +
+                 A.LE1v[2 * A.SV + js] * sX[ty + 1][tx + 3];
+            if (j == n1 - 1) {
+                acc = fma(0.5 * A.F1x[o], sX[ty + 1][tx], acc);
+                le += A.LE1x[o] * sX[ty + 1][tx];
+            }
         }
-        A.T[p] = a1;
-        A.W[p] = fma(0.5, a1, acc);
+        A.T[p] = le;
+        A.W[p] = acc;
         return;
     }
     if constexpr (MODE == ST_IMPLICIT) {
@@ -1296,6 +1328,7 @@ struct Layout {
         o_dirS;
     int64_t o_w0i, o_RSi, o_LSi, o_LVvi, o_foldVi, o_LVzi;
     int64_t o_FV, o_W, o_T, o_Y2, o_F0h, o_w0h, o_sw;
+    int64_t o_LE1v, o_LE1x, o_LE1z, o_one, o_F1h;
     int64_t bytes = 0;
     std::vector<int64_t> p_off, s_off, v_off, tile_off, task_off;
 };
@@ -1362,8 +1395,11 @@ static int make_layout(const fdadi_heston_batch_t *b, Layout &L) {
     if (L.hv) {
         L.o_FV = take(D * L.P); L.o_Y2 = take(D * L.P);
         L.o_F0h = take(3 * D * L.P); L.o_w0h = take(3 * D * L.SS);
+        L.o_LE1v = take(3 * D * L.SV); L.o_LE1x = take(D * N); L.o_LE1z = take(D * N);
+        L.o_one = take(D * N); L.o_F1h = take(3 * D * L.SV);
     } else {
         L.o_FV = L.o_Y2 = L.o_F0h = L.o_w0h = -1;
+        L.o_LE1v = L.o_LE1x = L.o_LE1z = L.o_one = L.o_F1h = -1;
     }
     L.bytes = off;
     return FDADI_OK;
@@ -1390,6 +1426,8 @@ static Arena arena_view(const Layout &L, char *ws) {
     A.foldVi = ptr(L.o_foldVi); A.LVzi = ptr(L.o_LVzi);
     A.FV = ptr(L.o_FV); A.W = ptr(L.o_W); A.T = ptr(L.o_T); A.Y2 = ptr(L.o_Y2);
     A.F0h = ptr(L.o_F0h); A.w0h = ptr(L.o_w0h); A.sw = ptr(L.o_sw);
+    A.LE1v = ptr(L.o_LE1v); A.LE1x = ptr(L.o_LE1x); A.LE1z = ptr(L.o_LE1z);
+    A.one = ptr(L.o_one); A.F1h = ptr(L.o_F1h);
     return A;
 }
 
@@ -1650,6 +1688,14 @@ static void launch_stage(int stage, const Grids &g, const Arena &A, double *V, c
 // One phase of a time step: an explicit stage and the two line solves after it.
 enum PhaseKind : int { PH_IMPLICIT, PH_DOUGLAS, PH_HV_PREDICT, PH_HV_CORRECT };
 
+// The HV corrector's T already holds theta dt A1 Y2 (reference rounding), so
+// its spot solve subtracts T with a factor of 1.
+static Arena corrector_solve_view(const Grids &g, const Arena &A) {
+    Arena B = A;
+    if (g.corr == ST_HV3) B.theta = A.one;
+    return B;
+}
+
 static void launch_phase(int kind, const Grids &g, const GroupSpan &s, const Arena &A, double *V,
                          cudaStream_t st, int prio) {
     switch (kind) {
@@ -1670,7 +1716,7 @@ static void launch_phase(int kind, const Grids &g, const GroupSpan &s, const Are
         break;
     default:
         launch_explicit(g.corr, s.tiles, g.expl_ctas, A, V, st);
-        launch_spot(g.si, false, s.lines, A, A.W, A.W, st, prio);
+        launch_spot(g.si, false, s.lines, corrector_solve_view(g, A), A.W, A.W, st, prio);
         launch_var(g.vi, false, s.tasks, A, A.W, V, st, prio);
         break;
     }
@@ -1792,7 +1838,8 @@ static int launch_steps(const fdadi_heston_batch_t *b, const Layout &L, const Ar
                 launch_var(g.vi, false, s.tasks, A, A.W, A.Y2, sk, g.prio_high);
                 break;
             default:
-                launch_spot(g.si, false, s.lines, A, A.W, A.W, sk, g.prio_high);
+                launch_spot(g.si, false, s.lines, corrector_solve_view(g, A), A.W, A.W, sk,
+                            g.prio_high);
                 launch_var(g.vi, false, s.tasks, A, A.W, V, sk, g.prio_high);
                 break;
             }
