@@ -549,7 +549,8 @@ __device__ __forceinline__ void explicit_tile(const Arena &A, const double *__re
     if constexpr (MODE == ST_HV3) {
         // Y0 - F(V - Y2)/2 - theta F0 Y2 = V + R + F(V)/2 + (1/2 - theta) F0 Y2
         //   + F1 Y2 / 2 + M Y2 / 2, accumulated in one FMA chain with the
-        // (1/2 - theta) F0 and w0 / 2 copies built for this stage
+        // (1/2 - theta) F0, F1 / 2 and w0 / 2 copies built for this stage (the
+        // halvings are exact)
         double acc = V[p];
         if (i == n0 - 1) acc += A.R0top[js];
         acc = fma(0.5, A.FV[p], acc);
@@ -567,12 +568,12 @@ __device__ __forceinline__ void explicit_tile(const Arena &A, const double *__re
             acc = fma(A.w0h[A.SS + so + i], sT[ty + 1][tx], acc);
             acc = fma(A.w0h[2 * A.SS + so + i], sT[ty + 2][tx], acc);
         }
-        // 1/2 F1 Y2 joins the chain through the halved copy of F1 (an exact
-        // scaling); the corrector's variance term theta dt A1 Y2 is formed
-        // apart, with the reference's (A1 theta) dt coefficients: these
-        // operators are built once, so a coefficient rounded otherwise (theta
-        // times dt A1, or 1/2 F1 taken from it) would bias every step alike,
-        // and over a run the price drifts by up to ~1e-10
+        // The corrector's variance term theta dt A1 Y2 is formed beside the
+        // chain's 1/2 F1 Y2 (same neighbours), with the reference's
+        // (A1 theta) dt coefficients: these operators are built once, so a
+        // coefficient rounded otherwise (theta times dt A1, or 1/2 F1 taken
+        // from it) would bias every step alike, and over a run the price
+        // drifts by up to ~1e-10.
         double le;
         if (i == 0 && (fl & OPT_ROW0_ZERO)) {
             acc = fma(0.5 * A.F1z[o], xc, acc);
