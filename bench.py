@@ -489,6 +489,26 @@ def run_surrogate(args):
     p = p.cpu().numpy()
     d = d.cpu().numpy()
     err = np.abs(p - pte)
+    gate = None
+    if args.gate:
+        # the error gate, trained on the training draws' own errors and
+        # calibrated on the first half of the held-out draws; judged on the
+        # second half and on the served query sample below
+        t0 = time.perf_counter()
+        sur.fit_gate(Qtr, ptr, epochs=args.epochs, batch=8192, lr=1e-3)
+        h = Qte.shape[0] // 2
+        tau, cal_fb = sur.calibrate(Qte[:h], pte[:h], bar=1e-3, margin=args.gate_margin)
+        _, _, _, fbv, _ = sur.predict(torch.as_tensor(Qte[h:], device=dev))
+        fbv = fbv.cpu().numpy().astype(bool)
+        ev = err[h:]
+        gate = {"bar": 1e-3, "threshold_log10": tau, "margin_log10": args.gate_margin,
+                "train_s": time.perf_counter() - t0,
+                "calibration_fallback_fraction": cal_fb,
+                "heldout_half_fallback_fraction": float(fbv.mean()),
+                "heldout_half_served_max_abs_err": float(ev[~fbv].max()) if (~fbv).any()
+                else None,
+                "heldout_half_misses_caught": float(fbv[ev > 1e-3].mean())
+                if (ev > 1e-3).any() else None}
     # queries: 95% in the box, 5% outside it
     rng = np.random.default_rng(args.seed + 3)
     nq = args.queries
@@ -498,21 +518,36 @@ def run_surrogate(args):
     Q[out, 6] = rng.uniform(0.1, 2.0, out.sum())
     def step():
         return sur.price(Q, pool=pool, **grid)
-    for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
-    times = []
-    for _ in range(args.steps):
-        t0 = time.perf_counter()
-        pq, dq, fbq = step()
+
+    def serve():
+        for _ in range(args.warmup):
+            step()
         torch.cuda.synchronize()
-        times.append(time.perf_counter() - t0)
-    value = nq / float(np.mean(times))
+        times = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            pq, dq, fbq = step()
+            torch.cuda.synchronize()
+            times.append(time.perf_counter() - t0)
+        return nq / float(np.mean(times)), times, pq, dq, fbq
+
+    value, times, pq, dq, fbq = serve()
     # accuracy of the served prices on a sample, against FP64 ADI
     ns = min(args.sample, nq)
     sidx = np.linspace(0, nq - 1, ns).astype(int)
     pref, _ = adi_price(Q[sidx], pool=pool, **grid)
     qerr = np.abs(pq[sidx] - pref)
+    box_only = None
+    if gate is not None:
+        # the other operating point: the box gate alone
+        tau = sur.gate_tau
+        sur.gate_tau = None
+        v2, t2, pq2, _, fbq2 = serve()
+        sur.gate_tau = tau
+        qerr2 = np.abs(pq2[sidx] - pref)
+        box_only = {"options_per_s": v2, "query_fallback_fraction": float(fbq2.mean()),
+                    "query_max_abs_err": float(qerr2.max()),
+                    "query_rms_abs_err": float(np.sqrt(np.mean(qerr2 ** 2)))}
     # tensor pipe: one ensemble forward on the query batch, timed with events
     Qd = torch.as_tensor(Q, device=dev)
     M = (nq // 128) * 128
@@ -560,6 +595,8 @@ def run_surrogate(args):
                                               "series in vol of variance (price), residual / "
                                               "(sigma sqrt T + 0.1)" % args.cv),
                           **alt,
+                          "error_gate": gate,
+                          "box_gate_only": box_only,
                           "adam_betas": list(sur.net.adam[:2]),
                           "train_data": cached or "priced in this run",
                           "data_gen_s": t_data, "train_s": t_train,
@@ -726,6 +763,10 @@ def main():
                          "run on the same seeds")
     ap.add_argument("--compare-cv", action="store_true",
                     help="also train on the same data with the other control variates")
+    ap.add_argument("--gate", action="store_true",
+                    help="surrogate: train and calibrate the error gate (served error <= 1e-3)")
+    ap.add_argument("--gate-margin", type=float, default=0.05,
+                    help="error gate: threshold margin below the calibration misses (log10)")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))

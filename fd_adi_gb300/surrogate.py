@@ -222,6 +222,31 @@ class Featurizer(object):
         return X, base, inbox
 
 
+def _train(net, X, T, epochs, batch, lr, seed, log):
+    """Adam over shuffled batches with a cosine learning rate (the training
+    recipe of every ensemble here). Returns the last batch loss per epoch."""
+    n = X.shape[0]
+    steps_per_epoch = max(1, n // batch)
+    total = epochs * steps_per_epoch
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    step = 0
+    losses = []
+    for ep in range(epochs):
+        perm = torch.randperm(n, generator=g).to(X.device)
+        ep_loss = 0.0
+        for s in range(steps_per_epoch):
+            idx = perm[s * batch:(s + 1) * batch]
+            lr_t = 0.5 * lr * (1 + math.cos(math.pi * step / total))
+            loss = net.train_step(X[idx].contiguous(), T[idx].contiguous(), batch, lr_t)
+            ep_loss += float(loss.mean().item()) if s == steps_per_epoch - 1 else 0.0
+            step += 1
+        losses.append(ep_loss)
+        if log:
+            log(ep, ep_loss)
+    net.check()
+    return losses
+
+
 def adi_price(queries, nS=256, nv=128, nt=200, chunk=4096, graph=False, spot_max_factor=8.0,
               var_max=5.0, pool=None):
     """FP64 ADI prices and deltas (HV theta = 1/2 + sqrt(3)/6 after two
@@ -285,6 +310,12 @@ class Surrogate(object):
         self.net = MLPEnsemble(members, seed, self.dev)
         self.feat = Featurizer(self.dev, cv)
         self.tol = tol
+        self.members = members
+        # error gate (fit_gate / calibrate): an ensemble predicting log10 of
+        # this surrogate's absolute price error, and the score above which a
+        # query falls back
+        self.gate_net = None
+        self.gate_tau = None
 
     def targets(self, Q, price, delta):
         """Scaled residual targets over the control variate (fp32 [n][2])."""
@@ -302,30 +333,58 @@ class Surrogate(object):
     def fit(self, Q, price, delta, epochs=50, batch=8192, lr=1e-3, seed=0, log=None):
         T = torch.as_tensor(self.targets(Q, price, delta), device=self.dev)
         X, _, _ = self.feat(torch.as_tensor(Q, device=self.dev))
-        n = Q.shape[0]
-        steps_per_epoch = max(1, n // batch)
-        total = epochs * steps_per_epoch
-        g = torch.Generator(device="cpu").manual_seed(seed)
-        step = 0
-        losses = []
-        for ep in range(epochs):
-            perm = torch.randperm(n, generator=g).to(self.dev)
-            ep_loss = 0.0
-            for s in range(steps_per_epoch):
-                idx = perm[s * batch:(s + 1) * batch]
-                lr_t = 0.5 * lr * (1 + math.cos(math.pi * step / total))
-                loss = self.net.train_step(X[idx].contiguous(), T[idx].contiguous(), batch, lr_t)
-                ep_loss += float(loss.mean().item()) if s == steps_per_epoch - 1 else 0.0
-                step += 1
-            losses.append(ep_loss)
-            if log:
-                log(ep, ep_loss)
-        self.net.check()
-        return losses
+        return _train(self.net, X, T, epochs, batch, lr, seed, log)
 
-    def predict(self, Q):
+    def fit_gate(self, Q, price, epochs=50, batch=8192, lr=1e-3, seed=7):
+        """Train the error gate: an ensemble of the same network, on the same
+        inputs, that predicts log10 of this surrogate's absolute price error,
+        fitted to the errors it makes on the training draws themselves (their
+        error equals the held-out error, so they are a fair sample of it)."""
+        Qd = torch.as_tensor(np.asarray(Q, dtype=np.float64), device=self.dev)
+        p = self.predict(Qd, gate=False)[0].cpu().numpy()
+        le = np.log10(np.abs(p - np.asarray(price)) + 1e-7)
+        self.gate_mu, self.gate_sd = float(le.mean()), float(max(le.std(), 1e-12))
+        T = torch.as_tensor(np.stack([(le - self.gate_mu) / self.gate_sd, np.zeros_like(le)], 1)
+                            .astype(np.float32), device=self.dev)
+        X, _, _ = self.feat(Qd)
+        self.gate_net = MLPEnsemble(self.members, seed, self.dev)
+        self.gate_net.loss_weights = torch.tensor([1.0, 0.0], dtype=torch.float32,
+                                                  device=self.dev)
+        self.gate_tau = None
+        return _train(self.gate_net, X, T, epochs, batch, lr, seed, None)
+
+    def gate_score(self, Q):
+        """Predicted log10 absolute price error of every query (device)."""
+        Q = Q.contiguous()
+        M0 = Q.shape[0]
+        M = ((M0 + 127) // 128) * 128
+        if M != M0:
+            Q = torch.cat([Q, Q[-1:].expand(M - M0, 9)], 0)
+        X, _, _ = self.feat(Q)
+        Y = self.gate_net.infer(X, M)
+        return Y[:, :M0, 0].to(torch.float64).mean(0) * self.gate_sd + self.gate_mu
+
+    def calibrate(self, Q, price, bar=1e-3, margin=0.05):
+        """Set the gate's threshold from calibration queries priced by ADI:
+        `margin` (log10 units) below the smallest score of any in-box query
+        whose surrogate price misses `bar`, so that every such query falls
+        back. Returns the threshold and the calibration fallback fraction."""
+        Qd = torch.as_tensor(np.asarray(Q, dtype=np.float64), device=self.dev)
+        p, _, _, fb, _ = self.predict(Qd, gate=False)
+        e = np.abs(p.cpu().numpy() - np.asarray(price))
+        g = self.gate_score(Qd).cpu().numpy()
+        inbox = ~fb.cpu().numpy().astype(bool)
+        bad = inbox & (e > bar)
+        self.gate_tau = float(g[bad].min() - margin) if bad.any() else float("inf")
+        self.gate_bar = bar
+        fall = (~inbox) | (g >= self.gate_tau)
+        return self.gate_tau, float(fall.mean())
+
+    def predict(self, Q, gate=True):
         """Q: [n][9] device float64. Returns (price, delta, spread, fallback
-        flags, fallback count) on the device."""
+        flags, fallback count) on the device. With a calibrated error gate
+        (and gate=True), queries whose predicted error reaches the threshold
+        fall back too."""
         Q = Q.contiguous()      # featurize and combine both read it as [n][9]
         M0 = Q.shape[0]
         M = ((M0 + 127) // 128) * 128
@@ -342,6 +401,11 @@ class Surrogate(object):
         _lib.call("fdadi_mlp_combine", _p(Y), 2, M * 2, self.net.P, M, _p(Q), _p(base),
                   _p(inbox), float(self.s[0]), float(self.s[1]), float(self.tol), _p(price),
                   _p(delta), _p(spread), _p(fb), _p(cnt), _st())
+        if gate and self.gate_net is not None and self.gate_tau is not None:
+            Yg = self.gate_net.infer(X, M)
+            g = Yg[:, :, 0].to(torch.float64).mean(0) * self.gate_sd + self.gate_mu
+            fb = (fb.bool() | (g >= self.gate_tau)).to(torch.int32)
+            cnt = fb[:M0].sum().to(torch.int32).reshape(1)
         return price[:M0], delta[:M0], spread[:M0], fb[:M0], cnt
 
     def price(self, Q_host, nS=256, nv=128, nt=200, pool=None):

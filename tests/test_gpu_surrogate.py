@@ -113,6 +113,24 @@ def test_surrogate_learns_adi_prices_and_gates(dev):
     Qout[:, 2] = 4.0                       # T beyond the box
     _, _, _, fbo, _ = sur.predict(torch.as_tensor(Qout, device=dev))
     assert bool(fbo.bool().all())
+    # the error gate: an ensemble predicting log10 |error|, calibrated on one
+    # half of the held-out draws so that every query there whose price misses
+    # the bar (the median error here: this short training is coarse) falls
+    # back; on the other half its scores must rank misses above hits
+    sur.fit_gate(Qtr, ptr, epochs=40, batch=512, lr=2e-3)
+    h = Qte.shape[0] // 2
+    e = np.abs(p - pte)
+    bar = float(np.median(e[:h]))
+    tau, frac = sur.calibrate(Qte[:h], pte[:h], bar=bar, margin=0.0)
+    _, _, _, fbg, cntg = sur.predict(torch.as_tensor(Qte, device=dev))
+    fbg = fbg.cpu().numpy().astype(bool)
+    assert int(cntg.item()) == int(fbg.sum())
+    assert fbg[:h][e[:h] > bar].all()          # every miss of the calibration half
+    assert 0.0 < frac < 1.0
+    g = sur.gate_score(torch.as_tensor(Qte[h:], device=dev)).cpu().numpy()
+    miss = e[h:] > bar
+    assert g[miss].mean() > g[~miss].mean()
+    sur.gate_tau = None
     # inference is much cheaper than pricing by ADI
     Qbig = torch.as_tensor(np.tile(Qte, (64, 1)), device=dev)
     sur.predict(Qbig)
