@@ -69,7 +69,7 @@ KERNEL_IO_BYTES = {"explicit_hv0": 32, "explicit_hv3": 40, "spot_solve": 24, "va
 # launch is this x points. The spot solve's figure includes its three Thomas
 # factors per point and the forward sweep's result read back by the backward
 # sweep, which the algorithmic state bytes leave out.
-NCU_TRAFFIC_B_PER_POINT = {"explicit_hv0": 52.7, "explicit_hv3": 62.3, "spot_solve": 56.9}
+NCU_TRAFFIC_B_PER_POINT = {"explicit_hv0": 52.6, "explicit_hv3": 62.6, "spot_solve": 56.9}
 # FP64 pipe work per grid point: FP64 instructions x 2, so that a pipe fully
 # busy with DFMA (2 flops each; DMUL and DADD occupy it the same) reads as the
 # DFMA peak that fdadi_fp64_probe measures. The mixed-term row sums are formed
