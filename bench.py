@@ -717,6 +717,173 @@ def run_reference(args, rank, world):
     return 0
 
 
+# Batched Black-Scholes (the 1-D engine): FP64 instructions per grid point per
+# step of the fused kernel: HV 23 (first sweep: F V 3, + V 1, Le V 3, - 1,
+# elimination 2; back substitution 1; second sweep: the difference 1, F D 3,
+# - 1/2 F D 1, Le Y1 3, - 1, elimination 2; back substitution 1); an implicit
+# step 3. State bytes per point per HV step, each array counted where the
+# kernel reads or writes it (operator rows and factors counted as cached):
+# V, Y0, D out of the first sweep (24), D in and Y1 out (16), V, Y1, Y0 in and
+# D out (32), D in and V out (16).
+BS_HV_INSTR, BS_IMPLICIT_INSTR, BS_HV_BYTES = 23, 3, 88
+
+
+def workload_bs(n_options, seed, nt=200):
+    """Seeded batched Black-Scholes calls: K/S0 in [0.7, 1.3], T in [0.1, 2],
+    r in [0, 0.08], volatility in [0.1, 0.6]; nS uniform over {64, 96, ...,
+    512}; meshes as the reference engine builds them (sinh to 1500 clustered at
+    S0 = 100)."""
+    rng = np.random.default_rng(seed)
+    K = 100.0 * rng.uniform(0.7, 1.3, n_options)
+    T = rng.uniform(0.1, 2.0, n_options)
+    r = rng.uniform(0.0, 0.08, n_options)
+    vol = rng.uniform(0.1, 0.6, n_options)
+    nS = rng.choice(np.arange(64, 513, 32), n_options).astype(np.int32)
+    return dict(S0=100.0, K=K, T=T, r=r, var=vol * vol, nS=nS, nt=nt)
+
+
+def run_bs(args):
+    """The batched Black-Scholes workload: price every option once per step
+    (operators built, payoff, the whole schedule in one launch, prices read)."""
+    import multiprocessing as mp
+    import torch
+    from fd_adi_gb300 import _lib, mesh as M
+    from fd_adi_gb300.batch import BlackScholesBatch
+    torch.cuda.set_device(0)
+    _lib.load()
+    n = args.bs_options
+    w = workload_bs(n, args.seed)
+    nt = w["nt"]
+    mesh_of = {int(k): np.asarray(M.sinh_space(100.0, 1500.0, 7.0, int(k), force_exact=True))
+               for k in np.unique(w["nS"])}
+    meshes = [mesh_of[int(k)] for k in w["nS"]]
+    params = np.stack([w["r"], w["var"]], axis=1)
+    dts = w["T"] / nt
+    batch = BlackScholesBatch([tuple(p) for p in params], meshes, scheme="hv", n_steps=nt - 1,
+                              dt=dts, theta=HV_THETA, implicit_steps=2, implicit_dt_factor=0.5)
+    K_dev = torch.tensor(w["K"], dtype=torch.float64, device="cuda")
+    flat_idx = batch.flat_index([100.0] * n)
+    prices = torch.empty(n, dtype=torch.float64, device="cuda")
+    V = torch.empty(batch.total_points, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def step_device():
+        batch._prepare()
+        batch.payoff(K_dev, V)
+        batch.run(V)
+        batch.gather(V, flat_idx, prices)
+
+    for _ in range(args.warmup):
+        step_device()
+    torch.cuda.synchronize()
+    clocks = Clocks(0)
+    clocks.start()
+    time.sleep(0.3)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step_device()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    # the run kernel alone (the whole schedule), events around its launch
+    r0, r1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    batch.payoff(K_dev, V)
+    r0.record(stream)
+    batch.run(V)
+    r1.record(stream)
+    torch.cuda.synchronize()
+    run_ms = r0.elapsed_time(r1)
+    # e2e: parameters in, prices out through the public call
+    batch.price_calls(100.0, w["K"], params, dts)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        got = batch.price_calls(100.0, w["K"], params, dts)
+    ms_e2e = (time.perf_counter() - t0) * 1e3 / args.steps
+    if not np.array_equal(got, prices.cpu().numpy()):
+        raise RuntimeError("price_calls differs from the device-resident step")
+    P = batch.total_points
+    instr = P * (2 * BS_IMPLICIT_INSTR + (nt - 1) * BS_HV_INSTR)
+    fp64, probe = fp64_peak(torch, 0)
+    fp_ach = 2.0 * instr / (run_ms * 1e-3) / 1e12
+    hbm_peak, peak_src = measured_peaks()
+    gbs = BS_HV_BYTES * P * (nt - 1) / (run_ms * 1e-3) / 1e9
+    out = {"metric": "Black-Scholes options/sec, batched FP64 ADI", "value": n / (ms * 1e-3),
+           "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": "batched Black-Scholes calls, uneven meshes, HV nt=200 with "
+                                  "Rannacher start", "options": n, "nt": nt,
+                      "grid_points": int(P), "nS": "uniform {64..512 step 32}",
+                      "mesh": "sinh_space(100, 1500, 7, nS, force_exact)",
+                      "scheme": "2 implicit half-steps + 199 HV steps, theta=1/2+sqrt(3)/6",
+                      "seed": args.seed, "parallelism": "dp1"},
+           "e2e": {"value": n / (ms_e2e * 1e-3), "unit": UNIT, "ms_per_step": ms_e2e,
+                   "h2d_bytes_per_step": int(batch.price_calls_h2d_bytes),
+                   "d2h_bytes_per_step": 8 * n,
+                   "api": "BlackScholesBatch.price_calls: host parameters in, host prices "
+                          "out (meshes built on the host, pinned copies, operators, payoff, "
+                          "one-launch schedule, read-out)"},
+           "gpu_launches": 4 * args.steps,
+           "grid_point_steps_per_s": float(P) * nt / (ms * 1e-3),
+           "roofline": {"bound": "fp64", "kernel": "bs_run_kernel (whole schedule)",
+                        "achieved": fp_ach, "peak": fp64, "unit": "TFLOP/s",
+                        "frac": fp_ach / fp64, "launch_ms": run_ms,
+                        "instructions_per_point_step": {"hv": BS_HV_INSTR,
+                                                        "implicit": BS_IMPLICIT_INSTR},
+                        "peak_source": "measured live: fdadi_fp64_probe",
+                        "traffic": None,
+                        "hbm": {"achieved": gbs, "peak": hbm_peak, "unit": "GB/s",
+                                "frac": gbs / hbm_peak, "bytes_per_point_step": BS_HV_BYTES,
+                                "peak_source": peak_src}},
+           "fp64_probe": probe, "clocks": clk}
+    if args.cpu_sample > 0:
+        from oracle import ref_harness as H
+        idx = sorted(set(np.linspace(0, n - 1, args.cpu_sample).astype(int).tolist()))
+        cores = os.cpu_count() or 1
+        if H.available():
+            for var in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
+                os.environ[var] = "1"
+            jobs = [(100.0, w["K"][k], w["r"][k], w["var"][k], w["T"][k], int(w["nS"][k]), nt)
+                    for k in idx]
+            with mp.get_context("spawn").Pool(min(cores, len(jobs))) as pool:
+                pool.map(H.price_bs_option, jobs[:1])
+                t0 = time.perf_counter()
+                res = pool.map(H.price_bs_option, jobs, chunksize=4)
+                el = time.perf_counter() - t0
+            ref = np.array([x[0] for x in res])
+            kind = "reference"
+            what = "reference CPU engine (compat build) with blackscholes.py's operator"
+        else:
+            from oracle import oracle as O
+            t0 = time.perf_counter()
+            ref = np.array([O.bs_solve(meshes[k], w["r"][k], w["var"][k],
+                                       np.maximum(meshes[k] - w["K"][k], 0.0),
+                                       [("implicit", 2, dts[k] / 2, 1.0),
+                                        ("hv", nt - 1, dts[k], HV_THETA)])[
+                                int(flat_idx[k].item() - batch.p_off[k])] for k in idx])
+            el = time.perf_counter() - t0
+            cores = 1
+            kind = "port"
+            what = "C restatement of the reference engine (oracle), one core"
+        mean_pts = float(np.mean(w["nS"]))
+        pts = float(sum(int(w["nS"][k]) for k in idx)) * nt
+        got = prices.cpu().numpy()[idx]
+        rel = np.abs(got - ref) / np.abs(ref)
+        out["cpu_baseline"] = {"value": pts / el / (mean_pts * nt), "unit": UNIT,
+                               "cores": min(cores, len(idx)), "kind": kind, "elapsed_s": el,
+                               "sample": "%s: %d options spread through the %d-option "
+                                         "workload on %d cores in %.1f s, scaled to the "
+                                         "workload's mean option"
+                                         % (what, len(idx), n, min(cores, len(idx)), el)}
+        out["parity"] = {"n": len(idx), "max_price_rel": float(rel.max()), "price_bar": 1e-10,
+                         "ok": bool(rel.max() <= 1e-10)}
+    print(json.dumps(out))
+    return 0
+
+
 def config_block(args, w):
     if args.workload == "large":
         return {"workload": "large single instance x3: K in {80,100,120}, 1024x512, nt=1000, "
@@ -749,7 +916,10 @@ def main():
                     help="line-solve launch plan from the size heuristic, not the autotuner")
     ap.add_argument("--plan", default=None,
                     help="launch plan as JSON (fdadi_heston_plan_t fields) instead of tuning")
-    ap.add_argument("--workload", default="batch", choices=["batch", "large", "surrogate", "gemm"])
+    ap.add_argument("--workload", default="batch",
+                    choices=["batch", "large", "surrogate", "gemm", "bs"])
+    ap.add_argument("--bs-options", type=int, default=65536,
+                    help="options of the batched Black-Scholes workload (--workload bs)")
     ap.add_argument("--train", type=int, default=1 << 17)
     ap.add_argument("--test", type=int, default=1 << 13)
     ap.add_argument("--queries", type=int, default=100000)
@@ -779,6 +949,8 @@ def main():
         return run_surrogate(args) if rank == 0 else 0
     if args.workload == "gemm":
         return run_gemm(args) if rank == 0 else 0
+    if args.workload == "bs":
+        return run_bs(args) if rank == 0 else 0
 
     import torch
     import torch.distributed as dist

@@ -84,6 +84,15 @@ class HestonBatch(ctypes.Structure):
                 ("rates", ctypes.c_void_p)]
 
 
+class BsBatch(ctypes.Structure):
+    """fdadi_bs_batch_t"""
+    _fields_ = [("n_options", ctypes.c_int32), ("scheme", ctypes.c_int32),
+                ("n_steps", ctypes.c_int32), ("implicit_steps", ctypes.c_int32),
+                ("theta", ctypes.c_double), ("implicit_dt_factor", ctypes.c_double),
+                ("n", ctypes.c_void_p), ("spots", ctypes.c_void_p),
+                ("params", ctypes.c_void_p), ("dt", ctypes.c_void_p)]
+
+
 class Gemm(ctypes.Structure):
     """fdadi_gemm_t"""
     _fields_ = [("A", ctypes.c_void_p), ("lda", ctypes.c_int64), ("strideA", ctypes.c_int64),
@@ -152,6 +161,17 @@ SIGNATURES = {
     "fdadi_heston_status": (ctypes.c_int, [ctypes.POINTER(HestonBatch), ctypes.c_void_p,
                                            ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
                                            ctypes.c_void_p]),
+    "fdadi_bs_workspace_bytes": (ctypes.c_int64, [ctypes.POINTER(BsBatch)]),
+    "fdadi_bs_prepare": (ctypes.c_int, [ctypes.POINTER(BsBatch), ctypes.c_void_p,
+                                        ctypes.c_int64, ctypes.c_void_p]),
+    "fdadi_bs_run": (ctypes.c_int, [ctypes.POINTER(BsBatch), ctypes.c_void_p, ctypes.c_int64,
+                                    ctypes.c_void_p, ctypes.c_void_p]),
+    "fdadi_bs_payoff": (ctypes.c_int, [ctypes.POINTER(BsBatch), ctypes.c_void_p,
+                                       ctypes.c_int64, ctypes.c_void_p, ctypes.c_int32,
+                                       ctypes.c_void_p, ctypes.c_void_p]),
+    "fdadi_bs_status": (ctypes.c_int, [ctypes.POINTER(BsBatch), ctypes.c_void_p,
+                                       ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
+                                       ctypes.c_void_p]),
     "fdadi_heston_stage": (ctypes.c_int, [ctypes.POINTER(HestonBatch), ctypes.c_void_p,
                                           ctypes.c_int64, ctypes.c_void_p, ctypes.c_int32,
                                           ctypes.c_void_p]),

@@ -506,3 +506,232 @@ def payoff_grids(options, meshes):
     """Call payoff max(S - K, 0) on each option's grid (heston.py:402)."""
     return [np.maximum(np.asarray(m[0])[:, None] - o.strike, 0.0) * np.ones((1, np.asarray(m[1]).size))
             for o, m in zip(options, meshes)]
+
+
+def bs_params(opt):
+    """(r, variance) of a Black-Scholes Option or a 2-sequence."""
+    if hasattr(opt, "interest_rate"):
+        return float(opt.interest_rate.value), float(opt.variance.value)
+    r, var = opt
+    return float(r), float(var)
+
+
+class BlackScholesBatch(object):
+    """Batched Black-Scholes on the fused engine (fdadi_bs_* in
+    include/fdadi.h): every option's operators and Thomas factors built on
+    the device once; ``run`` advances every option's whole schedule in one
+    launch (each option is one independent line).
+
+    options: Black-Scholes Option objects or (r, variance) tuples.
+    meshes:  list of spot meshes (numpy arrays, >= 4 points each).
+    dt:      per-option main step (scalar or sequence).
+    Schedule: ``implicit_steps`` fully implicit steps of dt*implicit_dt_factor,
+    then ``n_steps`` of ``scheme`` ("douglas", "hv", "cs" or "mcs") at ``theta``.
+    The operator is the reference's (blackscholes.py:144-239): r S D_S +
+    1/2 var S^2 D_SS - r, U = 0 at the first mesh point, dU/dS = 1 at S_max."""
+
+    def __init__(self, options, meshes, scheme="hv", n_steps=1, dt=0.01, theta=HV_THETA,
+                 implicit_steps=0, implicit_dt_factor=0.5, device=None, stream=None):
+        self.device = device or torch.device("cuda", torch.cuda.current_device())
+        n = len(options)
+        if n == 0 or len(meshes) != n:
+            raise ValueError("need one mesh per option")
+        self.options = options
+        self.n = n
+        self.sizes = np.array([np.asarray(m).size for m in meshes], dtype=np.int32)
+        if (self.sizes < 4).any():
+            raise ValueError("every spot mesh needs at least 4 points")
+        self.p_off = np.concatenate([[0], np.cumsum(self.sizes.astype(np.int64))]).astype(np.int64)
+        self.total_points = int(self.p_off[-1])
+        dev = self.device
+        self.spots = torch.as_tensor(np.concatenate([np.asarray(m, np.float64) for m in meshes]),
+                                     device=dev)
+        self.params = torch.as_tensor(np.array([bs_params(o) for o in options],
+                                               dtype=np.float64).reshape(n, 2), device=dev)
+        self.dt = torch.as_tensor(np.broadcast_to(np.asarray(dt, dtype=np.float64), (n,)).copy(),
+                                  device=dev)
+        self.stream = stream if stream is not None else torch.cuda.current_stream(dev)
+        if scheme not in SCHEMES:
+            raise ValueError("unknown scheme %r" % (scheme,))
+        self._n_host = self.sizes.copy()
+        self.struct = _lib.BsBatch(n, SCHEMES[scheme], int(n_steps), int(implicit_steps),
+                                   float(theta), float(implicit_dt_factor),
+                                   self._n_host.ctypes.data, self.spots.data_ptr(),
+                                   self.params.data_ptr(), self.dt.data_ptr())
+        nbytes = _lib.load().fdadi_bs_workspace_bytes(ctypes.byref(self.struct))
+        if nbytes < 0:
+            raise ValueError("bad batch: " + _lib.last_error())
+        self.workspace_bytes = int(nbytes)
+        self.workspace = torch.empty(self.workspace_bytes, dtype=torch.uint8, device=dev)
+        self._prepare()
+
+    @classmethod
+    def from_options(cls, options, nspots=100, spot_max=1500.0, spotdensity=7.0,
+                     force_exact=True, **kw):
+        """Meshes as the reference engine builds them (blackscholes.py:181-183):
+        sinh meshes on [0, ~spot_max] clustered at each option's spot."""
+        ns = np.broadcast_to(np.asarray(nspots), (len(options),))
+        meshes = [_mesh.sinh_space(o.spot, spot_max, spotdensity, int(k), force_exact=force_exact)
+                  for o, k in zip(options, ns)]
+        return cls(options, meshes, **kw), meshes
+
+    def _sptr(self):
+        return ctypes.c_void_p(self.stream.cuda_stream)
+
+    def _ws(self):
+        return ctypes.c_void_p(self.workspace.data_ptr())
+
+    def _prepare(self):
+        with torch.cuda.stream(self.stream):
+            _lib.call("fdadi_bs_prepare", ctypes.byref(self.struct), self._ws(),
+                      self.workspace_bytes, self._sptr())
+
+    def _check_state(self, V):
+        if (V.dtype != torch.float64 or not V.is_cuda or V.numel() != self.total_points
+                or not V.is_contiguous()):
+            raise ValueError("state must be a contiguous CUDA float64 tensor of %d points"
+                             % self.total_points)
+
+    def pack(self, grids):
+        """Host grids (one 1-D array per option) -> device state."""
+        flat = np.concatenate([np.asarray(g, dtype=np.float64).reshape(-1) for g in grids])
+        if flat.size != self.total_points:
+            raise ValueError("Dimension mismatch: %d grid points for a %d-point batch"
+                             % (flat.size, self.total_points))
+        return torch.as_tensor(flat, device=self.device)
+
+    def unpack(self, V):
+        h = V.detach().cpu().numpy()
+        return [h[self.p_off[k]:self.p_off[k + 1]].copy() for k in range(self.n)]
+
+    def run(self, V):
+        """Advance the packed state V (device, float64) in place: one launch."""
+        self._check_state(V)
+        self.stream.wait_stream(torch.cuda.current_stream(self.device))
+        _lib.call("fdadi_bs_run", ctypes.byref(self.struct), self._ws(), self.workspace_bytes,
+                  ctypes.c_void_p(V.data_ptr()), self._sptr())
+        torch.cuda.current_stream(self.device).wait_stream(self.stream)
+        return V
+
+    def solve(self, grids):
+        """Host grids in, host grids out."""
+        V = self.pack(grids)
+        self.run(V)
+        return self.unpack(V)
+
+    def payoff(self, strikes, V=None, put=False):
+        """Initial state max(S - K, 0) (or max(K - S, 0)) built on the device;
+        strikes: device float64 [n]."""
+        if (strikes.dtype != torch.float64 or not strikes.is_cuda or strikes.numel() != self.n
+                or not strikes.is_contiguous()):
+            raise ValueError("strikes must be a contiguous CUDA float64 tensor of %d values"
+                             % self.n)
+        if V is None:
+            V = torch.empty(self.total_points, dtype=torch.float64, device=self.device)
+        self._check_state(V)
+        _lib.call("fdadi_bs_payoff", ctypes.byref(self.struct), self._ws(), self.workspace_bytes,
+                  ctypes.c_void_p(strikes.data_ptr()), 1 if put else 0,
+                  ctypes.c_void_p(V.data_ptr()),
+                  ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream))
+        return V
+
+    def flat_index(self, spots=None):
+        """State index of each option's price point: the mesh point nearest its
+        spot (blackscholes.py:222-228, argmin |S - spot|)."""
+        if spots is None:
+            spots = [o.spot for o in self.options]
+        S = self.spots.cpu().numpy()
+        idx = np.array([self.p_off[k] + int(np.argmin(np.abs(S[self.p_off[k]:self.p_off[k + 1]]
+                                                              - spots[k])))
+                        for k in range(self.n)], dtype=np.int64)
+        return torch.as_tensor(idx, device=self.device)
+
+    def gather(self, V, flat_idx, out=None):
+        """V[flat_idx] on the device (the price read-out)."""
+        self._check_state(V)
+        HestonBatch._check_index(flat_idx)
+        if out is None:
+            out = torch.empty(flat_idx.numel(), dtype=torch.float64, device=self.device)
+        _lib.call("fdadi_gather", ctypes.c_void_p(V.data_ptr()),
+                  ctypes.c_void_p(flat_idx.data_ptr()), ctypes.c_void_p(out.data_ptr()),
+                  flat_idx.numel(),
+                  ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream))
+        return out
+
+    def status(self, V):
+        """Per-option status words (numpy int32), as HestonBatch.status."""
+        self._check_state(V)
+        out = torch.empty(self.n, dtype=torch.int32, device=self.device)
+        with torch.cuda.stream(self.stream):
+            _lib.call("fdadi_bs_status", ctypes.byref(self.struct), self._ws(),
+                      self.workspace_bytes, ctypes.c_void_p(V.data_ptr()),
+                      ctypes.c_void_p(out.data_ptr()), self._sptr())
+        self.stream.synchronize()
+        return out.cpu().numpy()
+
+    def price_calls(self, spot, strikes, params, dt, put=False, spot_max=1500.0,
+                    spotdensity=7.0, force_exact=True):
+        """Price a new set of options on this batch's mesh sizes, from their
+        parameters (host arrays in, host prices out), as the reference engine
+        does per option (blackscholes.py:181-183 builds the mesh, :222-232
+        reads the price): the sinh meshes (one per distinct spot and size),
+        the copies to the device, the operator build, payoff, run and price
+        read-out. spot: scalar or [n]; strikes, dt: [n]; params: [n, 2] of
+        (r, variance). Returns a numpy array of n prices."""
+        n = self.n
+        strikes = np.ascontiguousarray(strikes, dtype=np.float64).reshape(-1)
+        if strikes.size != n:
+            raise ValueError("need %d strikes, got %d" % (n, strikes.size))
+        spot = np.broadcast_to(np.asarray(spot, dtype=np.float64), (n,))
+        params = np.ascontiguousarray(params, dtype=np.float64).reshape(n, 2)
+        dt = np.broadcast_to(np.asarray(dt, dtype=np.float64), (n,))
+        cache = {}
+        spots = np.empty(self.total_points)
+        idx = np.empty(n, dtype=np.int64)
+        for k in range(n):
+            key = (float(spot[k]), int(self.sizes[k]))
+            if key not in cache:
+                S = np.asarray(_mesh.sinh_space(key[0], spot_max, spotdensity, key[1],
+                                                force_exact=force_exact), dtype=np.float64)
+                cache[key] = (S, int(np.argmin(np.abs(S - key[0]))))
+            S, i = cache[key]
+            spots[self.p_off[k]:self.p_off[k + 1]] = S
+            idx[k] = self.p_off[k] + i
+        if not hasattr(self, "_h"):
+            pin = lambda t: t.pin_memory()
+            self._h = dict(spots=pin(torch.empty(self.total_points, dtype=torch.float64)),
+                           params=pin(torch.empty(2 * n, dtype=torch.float64)),
+                           dt=pin(torch.empty(n, dtype=torch.float64)),
+                           K=pin(torch.empty(n, dtype=torch.float64)),
+                           idx=pin(torch.empty(n, dtype=torch.int64)),
+                           prices=pin(torch.empty(n, dtype=torch.float64)))
+            self._d = dict(K=torch.empty(n, dtype=torch.float64, device=self.device),
+                           idx=torch.empty(n, dtype=torch.int64, device=self.device),
+                           prices=torch.empty(n, dtype=torch.float64, device=self.device),
+                           V=torch.empty(self.total_points, dtype=torch.float64,
+                                         device=self.device))
+        h, d = self._h, self._d
+        h["spots"].numpy()[:] = spots
+        h["params"].numpy()[:] = params.reshape(-1)
+        h["dt"].numpy()[:] = dt
+        h["K"].numpy()[:] = strikes
+        h["idx"].numpy()[:] = idx
+        with torch.cuda.stream(self.stream):
+            self.stream.wait_stream(torch.cuda.current_stream(self.device))
+            self.spots.copy_(h["spots"], non_blocking=True)
+            self.params.view(-1).copy_(h["params"], non_blocking=True)
+            self.dt.copy_(h["dt"], non_blocking=True)
+            d["K"].copy_(h["K"], non_blocking=True)
+            d["idx"].copy_(h["idx"], non_blocking=True)
+            self._prepare()
+            self.payoff(d["K"], d["V"], put=put)
+            self.run(d["V"])
+            self.gather(d["V"], d["idx"], d["prices"])
+            h["prices"].copy_(d["prices"], non_blocking=True)
+        self.stream.synchronize()
+        return h["prices"].numpy().copy()
+
+    @property
+    def price_calls_h2d_bytes(self):
+        """Host-to-device bytes one price_calls() copies."""
+        return 8 * (self.total_points + 2 * self.n + 3 * self.n)

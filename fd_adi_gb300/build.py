@@ -12,7 +12,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libfdadi.so")
-SOURCES = ["fdadi_ops.cu", "fdadi_engine.cu", "fdadi_mlp.cu", "fdadi_mesh.cpp"]
+SOURCES = ["fdadi_ops.cu", "fdadi_engine.cu", "fdadi_bs.cu", "fdadi_mlp.cu", "fdadi_mesh.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
               "-I" + os.path.join(ROOT, "include")]

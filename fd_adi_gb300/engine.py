@@ -11,7 +11,9 @@
   (meshes, payoff grid, hard-coded Heston operators, ``idx``/``price``). Its
   ``solve_*`` wrappers run the fused batched engine (``HestonBatch``) by
   default; ``fused=False`` selects the per-operator path.
-* ``BlackScholesFiniteDifferenceEngine`` mirrors blackscholes.py:144-239.
+* ``BlackScholesFiniteDifferenceEngine`` mirrors blackscholes.py:144-239. Its
+  ``solve_*`` wrappers run the fused batched engine (``BlackScholesBatch``) by
+  default.
 
 Semantics follow the reference CPU engine (the oracle): the zero-derivative
 term -r/ndim is rounded to binary32 (BandedOperator.pxd:32 declares
@@ -627,10 +629,15 @@ class HestonFiniteDifferenceEngine(FiniteDifferenceEngineADI):
 
 
 class BlackScholesFiniteDifferenceEngine(FiniteDifferenceEngineADI):
-    """1-D Black-Scholes engine (blackscholes.py:144-239), non-log mesh."""
+    """1-D Black-Scholes engine (blackscholes.py:144-239), non-log mesh.
+
+    ``solve_*`` run the fused batched engine (``BlackScholesBatch``, the
+    whole schedule in one launch) by default; ``fused=False``, or custom
+    coefficients or boundaries, select the per-operator path."""
 
     def __init__(self, option, grid=None, spot_max=1500.0, nspots=100, spotdensity=7.0,
-                 force_exact=True, coefficients=None, boundaries=None, **kwargs):
+                 force_exact=True, coefficients=None, boundaries=None, fused=True, **kwargs):
+        self.fused = bool(fused) and not coefficients and not boundaries
         self.option = option
         r = option.interest_rate.value
         var = option.variance.value
@@ -656,6 +663,52 @@ class BlackScholesFiniteDifferenceEngine(FiniteDifferenceEngineADI):
     @property
     def price(self):
         return self.grid.domain[-1][self.idx]
+
+    # -- fused path --
+    def _fused_run(self, initial, scheme, n_steps, dt, theta, implicit_steps=0, factor=0.5):
+        from .batch import BlackScholesBatch
+        V0 = self.grid.domain[-1] if initial is None else initial
+        b = BlackScholesBatch([self.option], [self.spots], scheme=scheme, n_steps=n_steps,
+                              dt=[dt], theta=theta, implicit_steps=implicit_steps,
+                              implicit_dt_factor=factor)
+        out = b.solve([np.asarray(V0, dtype=float)])[0]
+        self.grid.domain.append(out.copy())
+        return out
+
+    def solve_implicit(self, n, dt, initial=None, callback=None, numpy=False):
+        if not self.fused:
+            return FiniteDifferenceEngineADI.solve_implicit(self, n, dt, initial, callback, numpy)
+        return self._fused_run(initial, "douglas", 0, dt, 0.5, int(n), 1.0)
+
+    def solve_douglas(self, n, dt, initial=None, theta=0.5, callback=None, numpy=False):
+        if not self.fused:
+            return FiniteDifferenceEngineADI.solve_douglas(self, n, dt, initial, theta)
+        return self._fused_run(initial, "douglas", int(n), dt, theta)
+
+    def solve_hundsdorferverwer(self, n, dt, initial=None, theta=0.5, callback=None,
+                                numpy=False):
+        if not self.fused:
+            return FiniteDifferenceEngineADI.solve_hundsdorferverwer(self, n, dt, initial, theta)
+        return self._fused_run(initial, "hv", int(n), dt, theta)
+
+    def solve_craigsneyd(self, n, dt, initial=None, theta=0.5, callback=None, numpy=False):
+        if not self.fused:
+            return FiniteDifferenceEngineADI.solve_craigsneyd(self, n, dt, initial, theta)
+        return self._fused_run(initial, "cs", int(n), dt, theta)
+
+    def solve_craigsneyd2(self, n, dt, initial=None, theta=0.5, callback=None, numpy=False):
+        if not self.fused:
+            return FiniteDifferenceEngineADI.solve_craigsneyd2(self, n, dt, initial, theta)
+        return self._fused_run(initial, "mcs", int(n), dt, theta)
+
+    def solve_smooth(self, n, dt, initial=None, callback=None, smoothing_steps=2, scheme=None):
+        if not self.fused:
+            return FiniteDifferenceEngineADI.solve_smooth(self, n, dt, initial, callback,
+                                                          smoothing_steps, scheme)
+        if scheme:
+            raise NotImplementedError("Changing smoothing schemes not supported on GPU.")
+        return self._fused_run(initial, "hv", int(n) - smoothing_steps, dt, 0.60,
+                               2 * smoothing_steps, 0.5)
 
 
 def heston_coefficients(r, kappa, theta, sigma, rho):

@@ -327,6 +327,53 @@ int fdadi_heston_greeks(const fdadi_heston_batch_t *batch, void *workspace,
 /* The plan fdadi_heston_run uses for this batch when batch->plan is NULL. */
 int fdadi_heston_default_plan(const fdadi_heston_batch_t *batch, fdadi_heston_plan_t *plan);
 
+/* ------------------------------------------------------------------------ */
+/* Fused batched Black-Scholes engine: the 1-D counterpart of the Heston    */
+/* batch. Replaces FiniteDifferenceEngineGPU's solve_* loops on the engine  */
+/* from_host_FiniteDifferenceEngine makes of a BlackScholesFiniteDifference */
+/* Engine (FiniteDifferenceEngineGPU.pyx:100-128, blackscholes.py:144-239): */
+/* A = r S D_S + 1/2 sigma^2 S^2 D_SS - r with U = 0 at the first mesh point */
+/* and dU/dS = 1 at S_max. Lines are independent, so one launch runs every  */
+/* option's whole schedule.                                                 */
+/* ------------------------------------------------------------------------ */
+typedef struct fdadi_bs_batch {
+    int32_t n_options;
+    int32_t scheme;          /* FDADI_SCHEME_DOUGLAS, _HV, _CS or _MCS (main segment) */
+    int32_t n_steps;         /* main-segment steps (0: implicit steps only) */
+    int32_t implicit_steps;  /* fully implicit steps run before the main segment */
+    double theta;            /* main-segment theta */
+    double implicit_dt_factor; /* implicit step = dt * factor (0.5: Rannacher half-steps) */
+    const int32_t *n;        /* HOST [n_options] spot points (>= 4) */
+    const double *spots;     /* DEVICE [sum n] spot meshes, packed */
+    const double *params;    /* DEVICE [n_options][2]: r, variance sigma^2 */
+    const double *dt;        /* DEVICE [n_options] main-segment step */
+} fdadi_bs_batch_t;
+
+/* Bytes of device workspace fdadi_bs_prepare/run need for this batch. */
+int64_t fdadi_bs_workspace_bytes(const fdadi_bs_batch_t *batch);
+
+/* Build every option's operators (F = dt A, Le = theta dt A) and the Thomas
+ * factors of 1 - theta dt A and of the implicit 1 - dt' A into the workspace. */
+int fdadi_bs_prepare(const fdadi_bs_batch_t *batch, void *workspace, int64_t workspace_bytes,
+                     void *stream);
+
+/* Run the schedule (implicit_steps fully implicit steps of dt*implicit_dt_factor,
+ * then n_steps of the scheme) on the packed state V (DEVICE [sum n], option k
+ * at offset sum_{m<k} n_m), in place: one kernel launch. */
+int fdadi_bs_run(const fdadi_bs_batch_t *batch, void *workspace, int64_t workspace_bytes,
+                 double *V, void *stream);
+
+/* Initial state: V = max(S - K, 0) (put == 0) or max(K - S, 0), strikes DEVICE
+ * double [n_options], V the packed state. */
+int fdadi_bs_payoff(const fdadi_bs_batch_t *batch, void *workspace, int64_t workspace_bytes,
+                    const double *strikes, int32_t put, double *V, void *stream);
+
+/* status[k] (DEVICE int32 [n_options]): FDADI_STATUS_PIVOT if a pivot of
+ * option k's line solves was zero or non-finite at prepare, FDADI_STATUS_NONFINITE
+ * if its state in V holds a NaN or infinity. */
+int fdadi_bs_status(const fdadi_bs_batch_t *batch, void *workspace, int64_t workspace_bytes,
+                    const double *V, int32_t *status, void *stream);
+
 /* FP64 throughput probe: every thread runs `chains` (1, 2, 4, 8 or 16)
  * independent DFMA chains for `iters` iterations; writes one value per thread
  * to out (>= blocks*threads doubles) and returns the number of floating-point

@@ -151,3 +151,37 @@ def price_option(job):
     t = time.perf_counter() - t0
     return (float(V[price_index(spots, vars_, S0, v0)]), float(nS) * nv * nt, t,
             np.asarray(V) if want_grid else None)
+
+
+def price_bs_option(job):
+    """Price one Black-Scholes call with the reference engine (for a process
+    pool): job = (S0, K, r, var, T, nS, nt[, want_grid]); the mesh as
+    BlackScholesFiniteDifferenceEngine builds it (blackscholes.py:181-183:
+    sinh_space(S0, 1500, 7, nS, force_exact=True)), its operator
+    (blackscholes.py:197-219) handed to the reference FiniteDifferenceEngineADI,
+    two implicit half-steps then HV theta = 1/2 + sqrt(3)/6. The price is the
+    grid value at the mesh point nearest S0 (blackscholes.py:222-228).
+    Returns (price, grid-point-steps, seconds of the time loop, grid or None)."""
+    import time
+    S0, K, r, var, T, nS, nt = job[:7]
+    want_grid = len(job) > 7 and bool(job[7])
+    FD, BO, U, Grid = _import()
+    spots = np.array(quiet(U.sinh_space, S0, 1500.0, 7.0, int(nS), force_exact=True),
+                     dtype=float)
+    coefficients = {(): lambda t: -r, (0,): lambda t, *d: r * d[0],
+                    (0, 0): lambda t, *d: 0.5 * var * d[0] ** 2}
+    boundaries = {(0,): ((0, lambda *a: 0.0), (1, lambda t, x: 1.0)),
+                  (0, 0): ((0, lambda *a: 0.0), (None, lambda t, x: 1.0))}
+    G = Grid([spots], initializer=lambda x: np.maximum(x - K, 0))
+    F = FD.FiniteDifferenceEngineADI(G, coefficients=coefficients, boundaries=boundaries,
+                                     schemes={})
+    quiet(F.init)
+    V0 = G.domain[-1].copy()
+    dt = T / nt
+    t0 = time.perf_counter()
+    V = quiet(F.solve_implicit, 2, dt * 0.5, initial=V0)
+    V = quiet(F.solve_hundsdorferverwer, int(nt) - 1, dt, initial=V,
+              theta=0.5 + np.sqrt(3.0) / 6.0)
+    t = time.perf_counter() - t0
+    i = int(np.argmin(np.abs(spots - S0)))
+    return (float(V[i]), float(nS) * nt, t, np.asarray(V) if want_grid else None)

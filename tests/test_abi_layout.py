@@ -17,7 +17,8 @@ HEADER = os.path.join(ROOT, "include", "fdadi.h")
 
 STRUCTS = [(_lib.Tri, "fdadi_tri_t"), (_lib.Mixed, "fdadi_mixed_t"),
            (_lib.MlpNet, "fdadi_mlp_net_t"), (_lib.HestonPlan, "fdadi_heston_plan_t"),
-           (_lib.HestonBatch, "fdadi_heston_batch_t"), (_lib.Gemm, "fdadi_gemm_t")]
+           (_lib.HestonBatch, "fdadi_heston_batch_t"), (_lib.Gemm, "fdadi_gemm_t"),
+           (_lib.BsBatch, "fdadi_bs_batch_t")]
 
 
 def _declarations():

@@ -161,3 +161,34 @@ def test_payoff_and_featurize_arguments():
     assert rc == 3 and "workspace too small" in _lib.last_error()
     rc = lib.fdadi_mlp_featurize(FAKE, 128, FAKE, FAKE, 5, FAKE, FAKE, FAKE, None)
     assert rc == 1 and "control variate" in _lib.last_error()
+
+
+def _bs(n, scheme=_lib.SCHEME_HV, n_steps=3, implicit=2):
+    n = np.asarray(n, np.int32)
+    return _lib.BsBatch(len(n), scheme, n_steps, implicit, 0.6, 0.5, n.ctypes.data, FAKE, FAKE,
+                        FAKE), n
+
+
+def test_black_scholes_batch_is_validated():
+    """fdadi_bs_*: lines shorter than 4 points, unknown schemes and negative
+    step counts are refused; the workspace holds 16 interleaved arrays padded
+    to each warp group's longest line (groups of 32, longest lines first)."""
+    lib = _lib.load()
+    b, keep = _bs([64, 3])
+    assert lib.fdadi_bs_workspace_bytes(ctypes.byref(b)) == -1
+    assert "4 spot points" in _lib.last_error()
+    b, keep = _bs([64], scheme=9)
+    assert lib.fdadi_bs_workspace_bytes(ctypes.byref(b)) == -1
+    assert "scheme" in _lib.last_error()
+    b, keep = _bs([64], n_steps=-1)
+    assert lib.fdadi_bs_workspace_bytes(ctypes.byref(b)) == -1
+    sizes = np.random.default_rng(0).integers(4, 300, 100)
+    b, keep = _bs(sizes)
+    got = lib.fdadi_bs_workspace_bytes(ctypes.byref(b))
+    srt = np.sort(sizes)[::-1]
+    ni = sum(32 * int(srt[g * 32]) for g in range((len(srt) + 31) // 32))
+    assert got >= 16 * 8 * ni
+    assert got < 16 * 8 * ni + 8 * 4096   # the per-slot tables are small
+    # the argument checks of the other entry points come before any launch
+    assert lib.fdadi_bs_prepare(ctypes.byref(b), None, got, None) != 0
+    assert lib.fdadi_bs_run(ctypes.byref(b), FAKE, got - 1, FAKE, None) == 3
