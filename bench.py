@@ -787,14 +787,23 @@ def run_bs(args):
     torch.cuda.synchronize()
     clk = clocks.stop()
     ms = e0.elapsed_time(e1) / args.steps
-    # the run kernel alone (the whole schedule), events around its launch
-    r0, r1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    batch.payoff(K_dev, V)
-    r0.record(stream)
-    batch.run(V)
-    r1.record(stream)
-    torch.cuda.synchronize()
-    run_ms = r0.elapsed_time(r1)
+    # the run kernel alone (the whole schedule), events around its launch;
+    # each prefetch depth once (the default choice is the batch's)
+    def run_once():
+        r0, r1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        batch.payoff(K_dev, V)
+        r0.record(stream)
+        batch.run(V)
+        r1.record(stream)
+        torch.cuda.synchronize()
+        return r0.elapsed_time(r1)
+
+    run_ms = run_once()
+    by_pf = {}
+    for pf in (1, 2):
+        batch.struct.prefetch = pf
+        by_pf[str(pf)] = round(run_once(), 3)
+    batch.struct.prefetch = 0
     # e2e: parameters in, prices out through the public call
     batch.price_calls(100.0, w["K"], params, dts)
     torch.cuda.synchronize()
@@ -831,6 +840,7 @@ def run_bs(args):
            "roofline": {"bound": "fp64", "kernel": "bs_run_kernel (whole schedule)",
                         "achieved": fp_ach, "peak": fp64, "unit": "TFLOP/s",
                         "frac": fp_ach / fp64, "launch_ms": run_ms,
+                        "launch_ms_by_prefetch": by_pf,
                         "instructions_per_point_step": {"hv": BS_HV_INSTR,
                                                         "implicit": BS_IMPLICIT_INSTR},
                         "peak_source": "measured live: fdadi_fp64_probe",

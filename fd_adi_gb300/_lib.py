@@ -90,7 +90,8 @@ class BsBatch(ctypes.Structure):
                 ("n_steps", ctypes.c_int32), ("implicit_steps", ctypes.c_int32),
                 ("theta", ctypes.c_double), ("implicit_dt_factor", ctypes.c_double),
                 ("n", ctypes.c_void_p), ("spots", ctypes.c_void_p),
-                ("params", ctypes.c_void_p), ("dt", ctypes.c_void_p)]
+                ("params", ctypes.c_void_p), ("dt", ctypes.c_void_p),
+                ("prefetch", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 class Gemm(ctypes.Structure):

@@ -528,10 +528,13 @@ class BlackScholesBatch(object):
     Schedule: ``implicit_steps`` fully implicit steps of dt*implicit_dt_factor,
     then ``n_steps`` of ``scheme`` ("douglas", "hv", "cs" or "mcs") at ``theta``.
     The operator is the reference's (blackscholes.py:144-239): r S D_S +
-    1/2 var S^2 D_SS - r, U = 0 at the first mesh point, dU/dS = 1 at S_max."""
+    1/2 var S^2 D_SS - r, U = 0 at the first mesh point, dU/dS = 1 at S_max.
+    prefetch: rows each thread loads ahead in its sweeps (1 or 2; 0 chooses by
+    batch size); the results do not depend on it."""
 
     def __init__(self, options, meshes, scheme="hv", n_steps=1, dt=0.01, theta=HV_THETA,
-                 implicit_steps=0, implicit_dt_factor=0.5, device=None, stream=None):
+                 implicit_steps=0, implicit_dt_factor=0.5, device=None, stream=None,
+                 prefetch=0):
         self.device = device or torch.device("cuda", torch.cuda.current_device())
         n = len(options)
         if n == 0 or len(meshes) != n:
@@ -557,7 +560,7 @@ class BlackScholesBatch(object):
         self.struct = _lib.BsBatch(n, SCHEMES[scheme], int(n_steps), int(implicit_steps),
                                    float(theta), float(implicit_dt_factor),
                                    self._n_host.ctypes.data, self.spots.data_ptr(),
-                                   self.params.data_ptr(), self.dt.data_ptr())
+                                   self.params.data_ptr(), self.dt.data_ptr(), int(prefetch), 0)
         nbytes = _lib.load().fdadi_bs_workspace_bytes(ctypes.byref(self.struct))
         if nbytes < 0:
             raise ValueError("bad batch: " + _lib.last_error())

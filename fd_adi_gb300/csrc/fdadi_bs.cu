@@ -8,9 +8,11 @@
 // with no synchronisation between steps.
 //
 // Layout: options are sorted by line length and dealt to slots of 32 (one
-// warp). A slot group's arrays are interleaved, element i of lane l at
-// base_g + 32 i + l, so every load and store of a warp covers 256 contiguous
-// bytes even though each lane walks its own line. The per-point operators
+// warp). A slot group's arrays are interleaved by row: array k of row i of
+// lane l sits at base_g + (16 i + k) 32 + l. Every load and store of a warp
+// covers 256 contiguous bytes even though each lane walks its own line, and
+// all 16 values of a row lie within 4 KB of one address register (the array
+// index is an immediate offset). The per-point operators
 // F = dt A, Le = theta dt A and the Thomas factors of 1 - theta dt A (and of
 // the implicit 1 - dt' A) are built once, with the reference's arithmetic
 // (fdadi_rows.cuh), so they equal the reference CPU engine's rows bit for bit.
@@ -31,7 +33,7 @@ namespace {
 constexpr int BS_LANES = 32;
 constexpr int BS_THREADS = 128;
 
-// Interleaved per-point arrays, in units of NI doubles.
+// Per-point arrays of a row (array k at offset 32 k within the row).
 enum : int {
     BA_V = 0,    // state
     BA_D = 1,    // forward-sweep results d'
@@ -44,22 +46,24 @@ enum : int {
     BA_COUNT = 16
 };
 
+constexpr int64_t ST = BS_LANES;             // stride between a row's arrays
+constexpr int64_t RS = BS_LANES * BA_COUNT;  // stride between rows of a line
+
 struct BsArena {
-    int64_t NI;                 // doubles per interleaved array
     int S;                      // slots (32 per group)
     const int *slot_opt;        // [S] option of the slot, -1 if empty
     const int *slot_n;          // [S] line length
-    const int64_t *slot_base;   // [S] index of element 0 (group base + lane)
+    const int64_t *slot_base;   // [S] index of row 0, array 0 (group base + lane)
     const int64_t *slot_soff;   // [S] offset of the option in the packed arrays
     double *RF;                 // [S] F's S_max residual: R dt
     double *RI;                 // [S] implicit operator's S_max residual: R (-dt')
     int *ostat;                 // [n_opt] status bits found at prepare
-    double *arr;                // [BA_COUNT][NI]
+    double *arr;                // [rows][BA_COUNT][32] per group
 };
 
 struct BsLayout {
     int n_opt = 0, n_groups = 0, S = 0;
-    int64_t NI = 0;
+    int64_t NI = 0;             // doubles of all groups' arrays
     std::vector<int> slot_opt, slot_n;
     std::vector<int64_t> slot_base, slot_soff;
     int64_t o_opt = 0, o_n = 0, o_base = 0, o_soff = 0, o_RF = 0, o_RI = 0, o_stat = 0,
@@ -107,7 +111,7 @@ int bs_layout(const fdadi_bs_batch_t *b, BsLayout &L) {
                 L.slot_soff[s] = soff[o];
             }
         }
-        base += (int64_t)BS_LANES * len;
+        base += (int64_t)BS_LANES * BA_COUNT * len;
     }
     L.NI = base;
     int64_t off = 0;
@@ -123,14 +127,13 @@ int bs_layout(const fdadi_bs_batch_t *b, BsLayout &L) {
     L.o_RF = take(8 * (int64_t)L.S);
     L.o_RI = take(8 * (int64_t)L.S);
     L.o_stat = take(4 * (int64_t)n);
-    L.o_arr = take(8 * (int64_t)BA_COUNT * L.NI);
+    L.o_arr = take(8 * L.NI);
     L.bytes = off;
     return FDADI_OK;
 }
 
 BsArena bs_view(const BsLayout &L, char *ws) {
     BsArena A;
-    A.NI = L.NI;
     A.S = L.S;
     A.slot_opt = (const int *)(ws + L.o_opt);
     A.slot_n = (const int *)(ws + L.o_n);
@@ -179,14 +182,13 @@ __global__ void bs_build_kernel(BsArena A, BsBuild a) {
     const double dt = a.dt[o];
     const float minus_r = (float)(-r / 1.0);
     const double sm = MUL(a.theta, -dt), si = -MUL(dt, a.dt_factor);
-    const int64_t NI = A.NI, b = A.slot_base[s];
-    double *arr = A.arr;
+    double *p = A.arr + A.slot_base[s];
     Thomas tm, ti;
     for (int i = 0; i < n; ++i) {
         double w[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
         spot_weights(S, n, i, w, 1);
         const Row3 row = spot_row_w(w, 1, S, n, i, var, r, minus_r, false);
-        const int64_t q = b + (int64_t)BS_LANES * i;
+        const int64_t q = (int64_t)i * RS;
         double f[3], e[3], m[3], im[3];
         if (row.dirichlet) {
             f[0] = e[0] = m[0] = im[0] = 0.0;
@@ -204,11 +206,11 @@ __global__ void bs_build_kernel(BsArena A, BsBuild a) {
             im[1] = ADD(im[1], 1.0);
         }
         for (int k = 0; k < 3; ++k) {
-            arr[(BA_F + k) * NI + q] = f[k];
-            arr[(BA_LE + k) * NI + q] = e[k];
+            p[q + (BA_F + k) * ST] = f[k];
+            p[q + (BA_LE + k) * ST] = e[k];
         }
-        tm.row(arr + BA_LM * NI, NI, q, m[0], m[1], m[2], i == 0);
-        ti.row(arr + BA_LI * NI, NI, q, im[0], im[1], im[2], i == 0);
+        tm.row(p, ST, q + BA_LM * ST, m[0], m[1], m[2], i == 0);
+        ti.row(p, ST, q + BA_LI * ST, im[0], im[1], im[2], i == 0);
         if (i == n - 1) {
             A.RF[s] = MUL(row.R, dt);
             A.RI[s] = MUL(row.R, si);
@@ -217,96 +219,133 @@ __global__ void bs_build_kernel(BsArena A, BsBuild a) {
     A.ostat[o] = (tm.bad || ti.bad) ? FDADI_STATUS_PIVOT : 0;
 }
 
-// One lane's line: element i of array k at arr[k NI + base + 32 i].
+// One lane's line: array k of row i at p[RS i + ST k].
 struct BsLine {
-    double *arr;
-    int64_t NI, base;
+    double *p;
     int n;
-    __device__ __forceinline__ double *at(int k) const { return arr + k * NI + base; }
+    __device__ __forceinline__ double &at(int i, int k) const { return p[(int64_t)i * RS + k * ST]; }
 };
 
-constexpr int64_t ST = BS_LANES;  // element stride of a line
+// Rows are loaded PF ahead of the row being eliminated: every row's loads are
+// independent of the recurrence, so PF of them stay in flight while the
+// thread computes (one thread walks a whole line; with few options per SM
+// nothing else would hide the memory latency). Runs body(i, row) for
+// i = lo, lo + dir, ... (count rows), row = load(i).
+template <int PF, class Row, class Load, class Body>
+__device__ __forceinline__ void pipelined(int lo, int count, int dir, Load load, Body body) {
+    Row ring[PF];
+#pragma unroll
+    for (int d = 0; d < PF; ++d)
+        if (d < count) ring[d] = load(lo + d * dir);
+    for (int k0 = 0; k0 < count; k0 += PF) {
+#pragma unroll
+        for (int d = 0; d < PF; ++d) {
+            const int k = k0 + d;
+            if (k < count) {
+                body(lo + k * dir, ring[d]);
+                if (k + PF < count) ring[d] = load(lo + (k + PF) * dir);
+            }
+        }
+    }
+}
 
-// y = F x on row i (1 <= i <= n-1) with x[-1] forced to the Dirichlet value 0
+
+// y = c x on row i (1 <= i <= n-1) with x[-1] forced to the Dirichlet value 0
 // (apply, BandedOperator.pyx:331-361: force_dirichlet, then the DIA
-// matvec's diagonal order +1, 0, -1).
-__device__ __forceinline__ double row_apply(const double *c, int64_t NI, int64_t q, bool top,
+// matvec's diagonal order +1, 0, -1); the last row has no +1 entry.
+__device__ __forceinline__ double row_apply(double sub, double mid, double sup, bool top,
                                             double xm, double x0, double xp) {
-    const double sub = c[q], mid = c[NI + q];
-    double acc = top ? mid * x0 : fma(mid, x0, c[2 * NI + q] * xp);
+    const double acc = top ? mid * x0 : fma(mid, x0, sup * xp);
     return fma(sub, xm, acc);
 }
 
-// Thomas forward sweep of the rows 1..n-1 given their right-hand sides; row
-// 0 is the Dirichlet row (forced to 0, so d'_0 = 0).
+// One row's operands in a forward sweep: the next state value(s), the rows
+// of F and Le, the elimination factors and (second HV sweep) Y0.
+struct SweepRow {
+    double xp, yp, y0, f0, f1, f2, e0, e1, e2, a, inv;
+};
+
+template <bool WITH_Y>
+__device__ __forceinline__ SweepRow load_sweep(const BsLine &l, int i) {
+    const double *q = l.p + (int64_t)i * RS;
+    const bool top = i == l.n - 1;
+    SweepRow r;
+    r.xp = top ? 0.0 : q[RS + BA_V * ST];
+    r.yp = (WITH_Y && !top) ? q[RS + BA_Y1 * ST] : 0.0;
+    r.y0 = WITH_Y ? q[BA_Y0 * ST] : 0.0;
+    r.f0 = q[BA_F * ST];
+    r.f1 = q[(BA_F + 1) * ST];
+    r.f2 = top ? 0.0 : q[(BA_F + 2) * ST];
+    r.e0 = q[BA_LE * ST];
+    r.e1 = q[(BA_LE + 1) * ST];
+    r.e2 = top ? 0.0 : q[(BA_LE + 2) * ST];
+    r.a = q[BA_LM * ST];
+    r.inv = q[(BA_LM + 1) * ST];
+    return r;
+}
+
+struct BackRow {
+    double d, cp;
+};
+
+// Back substitution x_i = d'_i - c'_i x_{i+1} into array k (factors of
+// array fac), from x_{n-1} = d'_{n-1} = dp.
+template <int PF>
+__device__ __forceinline__ void back_into(const BsLine &l, double dp, int k, int fac) {
+    const int n = l.n;
+    l.at(n - 1, k) = dp;
+    double x = dp;
+    pipelined<PF, BackRow>(
+        n - 2, n - 1, -1,
+        [&](int i) { return BackRow{l.at(i, BA_D), l.at(i, fac + 2)}; },
+        [&](int i, const BackRow &r) {
+            x = r.d - r.cp * x;
+            l.at(i, k) = x;
+        });
+}
+
 // Douglas (and Craig-Sneyd, which in one dimension without a mixed term
 // repeats the Douglas sweep and keeps its result): V <- Li^-1 (V + F V - Le V).
+// Row 0 is the Dirichlet row, forced to 0 (d'_0 = 0).
+template <int PF>
 __device__ void bs_douglas(const BsLine &l, double rf) {
     const int n = l.n;
-    const double *V = l.at(BA_V);
-    double *D = l.at(BA_D);
-    const double *F = l.at(BA_F), *E = l.at(BA_LE), *M = l.at(BA_LM);
-    const int64_t NI = l.NI;
-    double xm = 0.0, x0 = V[ST], dp = 0.0;
-    D[0] = 0.0;
-    for (int i = 1; i < n; ++i) {
-        const int64_t q = i * ST;
-        const bool top = i == n - 1;
-        const double xp = top ? 0.0 : V[q + ST];
-        double y = x0 + (row_apply(F, NI, q, top, xm, x0, xp) + (top ? rf : 0.0));
-        y = y - row_apply(E, NI, q, top, xm, x0, xp);
-        dp = (y - M[q] * dp) * M[NI + q];
-        D[q] = dp;
-        xm = x0;
-        x0 = xp;
-    }
-    double *Vw = l.at(BA_V);
-    double x = dp;
-    Vw[(n - 1) * ST] = x;
-    for (int i = n - 2; i >= 0; --i) {
-        const int64_t q = i * ST;
-        x = D[q] - M[2 * NI + q] * x;
-        Vw[q] = x;
-    }
+    double xm = 0.0, x0 = l.at(1, BA_V), dp = 0.0;
+    l.at(0, BA_D) = 0.0;
+    pipelined<PF, SweepRow>(
+        1, n - 1, 1, [&](int i) { return load_sweep<false>(l, i); },
+        [&](int i, const SweepRow &r) {
+            const bool top = i == n - 1;
+            double y = x0 + (row_apply(r.f0, r.f1, r.f2, top, xm, x0, r.xp) + (top ? rf : 0.0));
+            y = y - row_apply(r.e0, r.e1, r.e2, top, xm, x0, r.xp);
+            dp = (y - r.a * dp) * r.inv;
+            l.at(i, BA_D) = dp;
+            xm = x0;
+            x0 = r.xp;
+        });
+    back_into<PF>(l, dp, BA_V, BA_LM);
 }
+
+struct ImplicitRow {
+    double v, a, inv;
+};
 
 // Implicit step: V <- (1 - dt' A)^-1 (V - R_i) with the residual on the
 // S_max row (solve, BandedOperator.pyx:364-394).
+template <int PF>
 __device__ void bs_implicit(const BsLine &l, double ri) {
     const int n = l.n;
-    double *V = l.at(BA_V), *D = l.at(BA_D);
-    const double *M = l.at(BA_LI);
-    const int64_t NI = l.NI;
     double dp = 0.0;
-    D[0] = 0.0;
-    for (int i = 1; i < n; ++i) {
-        const int64_t q = i * ST;
-        double y = V[q];
-        if (i == n - 1) y = y - ri;
-        dp = (y - M[q] * dp) * M[NI + q];
-        D[q] = dp;
-    }
-    double x = dp;
-    V[(n - 1) * ST] = x;
-    for (int i = n - 2; i >= 0; --i) {
-        const int64_t q = i * ST;
-        x = D[q] - M[2 * NI + q] * x;
-        V[q] = x;
-    }
-}
-
-// Backward sweep into array k from the forward results in D.
-__device__ __forceinline__ void back_into(const BsLine &l, double dp, int k) {
-    const int n = l.n;
-    const double *D = l.at(BA_D), *M = l.at(BA_LM);
-    double *Y = l.at(k);
-    double x = dp;
-    Y[(n - 1) * ST] = x;
-    for (int i = n - 2; i >= 0; --i) {
-        const int64_t q = i * ST;
-        x = D[q] - M[2 * l.NI + q] * x;
-        Y[q] = x;
-    }
+    l.at(0, BA_D) = 0.0;
+    pipelined<PF, ImplicitRow>(
+        1, n - 1, 1,
+        [&](int i) { return ImplicitRow{l.at(i, BA_V), l.at(i, BA_LI), l.at(i, BA_LI + 1)}; },
+        [&](int i, const ImplicitRow &r) {
+            const double y = i == n - 1 ? r.v - ri : r.v;
+            dp = (y - r.a * dp) * r.inv;
+            l.at(i, BA_D) = dp;
+        });
+    back_into<PF>(l, dp, BA_V, BA_LI);
 }
 
 // HV in one dimension (FiniteDifferenceEngine.pyx:700-775):
@@ -316,54 +355,54 @@ __device__ __forceinline__ void back_into(const BsLine &l, double dp, int k) {
 // no mixed term:
 //   Y0 = V + F V, Y1 = Li^-1 (Y0 - Le V),
 //   V <- Li^-1 (Y0 + (1/2 - theta) F (Y1 - V) - Le V), F with its residual.
-template <bool MCS>
+template <bool MCS, int PF>
 __device__ void bs_two_sweeps(const BsLine &l, double rf, double c) {
     const int n = l.n;
-    const int64_t NI = l.NI;
-    const double *V = l.at(BA_V), *F = l.at(BA_F), *E = l.at(BA_LE), *M = l.at(BA_LM);
-    double *D = l.at(BA_D), *Y0 = l.at(BA_Y0);
-    double xm = 0.0, x0 = V[ST], dp = 0.0;
-    D[0] = 0.0;
-    for (int i = 1; i < n; ++i) {
-        const int64_t q = i * ST;
-        const bool top = i == n - 1;
-        const double xp = top ? 0.0 : V[q + ST];
-        const double y0 = x0 + (row_apply(F, NI, q, top, xm, x0, xp) + (top ? rf : 0.0));
-        Y0[q] = y0;
-        const double z = y0 - row_apply(E, NI, q, top, xm, x0, xp);
-        dp = (z - M[q] * dp) * M[NI + q];
-        D[q] = dp;
-        xm = x0;
-        x0 = xp;
-    }
-    back_into(l, dp, BA_Y1);
-    const double *Y1 = l.at(BA_Y1);
+    const double v1 = l.at(1, BA_V);
+    double xm = 0.0, x0 = v1, dp = 0.0;
+    l.at(0, BA_D) = 0.0;
+    pipelined<PF, SweepRow>(
+        1, n - 1, 1, [&](int i) { return load_sweep<false>(l, i); },
+        [&](int i, const SweepRow &r) {
+            const bool top = i == n - 1;
+            const double y0 =
+                x0 + (row_apply(r.f0, r.f1, r.f2, top, xm, x0, r.xp) + (top ? rf : 0.0));
+            l.at(i, BA_Y0) = y0;
+            const double z = y0 - row_apply(r.e0, r.e1, r.e2, top, xm, x0, r.xp);
+            dp = (z - r.a * dp) * r.inv;
+            l.at(i, BA_D) = dp;
+            xm = x0;
+            x0 = r.xp;
+        });
+    back_into<PF>(l, dp, BA_Y1, BA_LM);
     // second sweep: differences D = V - Y1 (HV) or Y1 - V (MCS), each formed
     // once and carried along the window; the Dirichlet row's is forced to 0
-    double vm = 0.0, v0 = V[ST], ym = 0.0, y0r = Y1[ST];
+    const double y1 = l.at(1, BA_Y1);
+    double vm = 0.0, v0 = v1, ym = 0.0, y0r = y1;
     double dm = 0.0, d0 = MCS ? y0r - v0 : v0 - y0r;
     dp = 0.0;
-    for (int i = 1; i < n; ++i) {
-        const int64_t q = i * ST;
-        const bool top = i == n - 1;
-        const double vp = top ? 0.0 : V[q + ST], yp = top ? 0.0 : Y1[q + ST];
-        const double dpn = top ? 0.0 : (MCS ? yp - vp : vp - yp);
-        const double fd = row_apply(F, NI, q, top, dm, d0, dpn);
-        double w;
-        if (MCS) {
-            w = fma(c, fd + (top ? rf : 0.0), Y0[q]);
-            w = w - row_apply(E, NI, q, top, vm, v0, vp);
-        } else {
-            w = fma(-0.5, fd, Y0[q]);
-            w = w - row_apply(E, NI, q, top, ym, y0r, yp);
-        }
-        dp = (w - M[q] * dp) * M[NI + q];
-        D[q] = dp;
-        vm = v0; v0 = vp;
-        ym = y0r; y0r = yp;
-        dm = d0; d0 = dpn;
-    }
-    back_into(l, dp, BA_V);
+    pipelined<PF, SweepRow>(
+        1, n - 1, 1, [&](int i) { return load_sweep<true>(l, i); },
+        [&](int i, const SweepRow &r) {
+            const bool top = i == n - 1;
+            const double vp = r.xp, yp = r.yp;
+            const double dpn = top ? 0.0 : (MCS ? yp - vp : vp - yp);
+            const double fd = row_apply(r.f0, r.f1, r.f2, top, dm, d0, dpn);
+            double w;
+            if (MCS) {
+                w = fma(c, fd + (top ? rf : 0.0), r.y0);
+                w = w - row_apply(r.e0, r.e1, r.e2, top, vm, v0, vp);
+            } else {
+                w = fma(-0.5, fd, r.y0);
+                w = w - row_apply(r.e0, r.e1, r.e2, top, ym, y0r, yp);
+            }
+            dp = (w - r.a * dp) * r.inv;
+            l.at(i, BA_D) = dp;
+            vm = v0; v0 = vp;
+            ym = y0r; y0r = yp;
+            dm = d0; d0 = dpn;
+        });
+    back_into<PF>(l, dp, BA_V, BA_LM);
 }
 
 struct BsSched {
@@ -373,23 +412,25 @@ struct BsSched {
 
 // One thread per slot: copy the option's packed state into its interleaved
 // line, run the whole schedule, copy the result back.
-__global__ void __launch_bounds__(BS_THREADS) bs_run_kernel(BsArena A, double *Vp, BsSched sc) {
+// Four blocks per SM (at most 128 registers a thread): 65,536 options (2048
+// warps) stay resident in one wave.
+template <int PF>
+__global__ void __launch_bounds__(BS_THREADS, 4) bs_run_kernel(BsArena A, double *Vp, BsSched sc) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= A.S) return;
     if (A.slot_opt[s] < 0) return;
-    BsLine l{A.arr, A.NI, A.slot_base[s], A.slot_n[s]};
-    double *V = l.at(BA_V);
+    const BsLine l{A.arr + A.slot_base[s], A.slot_n[s]};
     double *src = Vp + A.slot_soff[s];
-    for (int i = 0; i < l.n; ++i) V[i * ST] = src[i];
+    for (int i = 0; i < l.n; ++i) l.at(i, BA_V) = src[i];
     const double rf = A.RF[s], ri = A.RI[s];
-    for (int k = 0; k < sc.implicit_steps; ++k) bs_implicit(l, ri);
+    for (int k = 0; k < sc.implicit_steps; ++k) bs_implicit<PF>(l, ri);
     const double c = 0.5 - sc.theta;
     for (int k = 0; k < sc.n_steps; ++k) {
-        if (sc.scheme == FDADI_SCHEME_HV) bs_two_sweeps<false>(l, rf, c);
-        else if (sc.scheme == FDADI_SCHEME_MCS) bs_two_sweeps<true>(l, rf, c);
-        else bs_douglas(l, rf);
+        if (sc.scheme == FDADI_SCHEME_HV) bs_two_sweeps<false, PF>(l, rf, c);
+        else if (sc.scheme == FDADI_SCHEME_MCS) bs_two_sweeps<true, PF>(l, rf, c);
+        else bs_douglas<PF>(l, rf);
     }
-    for (int i = 0; i < l.n; ++i) src[i] = V[i * ST];
+    for (int i = 0; i < l.n; ++i) src[i] = l.at(i, BA_V);
 }
 
 // One block per option: V = max(S - K, 0) or max(K - S, 0).
@@ -466,9 +507,18 @@ int fdadi_bs_run(const fdadi_bs_batch_t *b, void *ws, int64_t bytes, double *V, 
     int rc = bs_begin(b, ws, bytes, L);
     if (rc) return rc;
     FDADI_REQUIRE(V != nullptr, "null state");
+    FDADI_REQUIRE(b->prefetch >= 0 && b->prefetch <= 2,
+                  "prefetch must be 0 (by batch size), 1 or 2");
     BsSched sc{b->scheme, b->n_steps, b->implicit_steps, b->theta};
-    bs_run_kernel<<<(L.S + BS_THREADS - 1) / BS_THREADS, BS_THREADS, 0, as_stream(stream)>>>(
-        bs_view(L, (char *)ws), V, sc);
+    // rows in flight per thread: with few warps per SM nothing else hides the
+    // memory latency, with many the plain loop keeps registers for occupancy
+    int pf = b->prefetch;
+    if (pf == 0) pf = L.n_groups >= 8 * sm_count() ? 1 : 2;
+    const unsigned grid = (L.S + BS_THREADS - 1) / BS_THREADS;
+    cudaStream_t st = as_stream(stream);
+    const BsArena A = bs_view(L, (char *)ws);
+    if (pf == 1) bs_run_kernel<1><<<grid, BS_THREADS, 0, st>>>(A, V, sc);
+    else bs_run_kernel<2><<<grid, BS_THREADS, 0, st>>>(A, V, sc);
     FDADI_CHECK_LAUNCH();
     return FDADI_OK;
 }

@@ -115,6 +115,12 @@ def test_uneven_batch_vs_oracle(cuda, scheme):
     b = BlackScholesBatch([(o["r"], o["var"]) for o in opts], meshes, dt=dts, **kw)
     V0 = [np.maximum(S - o["K"], 0.0) for o, S in zip(opts, meshes)]
     got = b.solve(V0)
+    # both prefetch depths run the same arithmetic: identical bits
+    for pf in (1, 2):
+        other = BlackScholesBatch([(o["r"], o["var"]) for o in opts], meshes, dt=dts,
+                                  prefetch=pf, **kw).solve(V0)
+        for x, y in zip(got, other):
+            np.testing.assert_array_equal(x, y)
     for k, (o, S) in enumerate(zip(opts, meshes)):
         ref = O.bs_solve(S, o["r"], o["var"], V0[k], sched[k])
         assert _rel(got[k], ref) <= 1e-11, (scheme, k, S.size, _rel(got[k], ref))

@@ -166,7 +166,7 @@ def test_payoff_and_featurize_arguments():
 def _bs(n, scheme=_lib.SCHEME_HV, n_steps=3, implicit=2):
     n = np.asarray(n, np.int32)
     return _lib.BsBatch(len(n), scheme, n_steps, implicit, 0.6, 0.5, n.ctypes.data, FAKE, FAKE,
-                        FAKE), n
+                        FAKE, 0, 0), n
 
 
 def test_black_scholes_batch_is_validated():
@@ -192,3 +192,6 @@ def test_black_scholes_batch_is_validated():
     # the argument checks of the other entry points come before any launch
     assert lib.fdadi_bs_prepare(ctypes.byref(b), None, got, None) != 0
     assert lib.fdadi_bs_run(ctypes.byref(b), FAKE, got - 1, FAKE, None) == 3
+    b.prefetch = 3
+    assert lib.fdadi_bs_run(ctypes.byref(b), FAKE, got, FAKE, None) == 1
+    assert "prefetch" in _lib.last_error()
