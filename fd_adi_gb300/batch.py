@@ -688,18 +688,18 @@ class BlackScholesBatch(object):
         spot = np.broadcast_to(np.asarray(spot, dtype=np.float64), (n,))
         params = np.ascontiguousarray(params, dtype=np.float64).reshape(n, 2)
         dt = np.broadcast_to(np.asarray(dt, dtype=np.float64), (n,))
-        cache = {}
         spots = np.empty(self.total_points)
         idx = np.empty(n, dtype=np.int64)
-        for k in range(n):
-            key = (float(spot[k]), int(self.sizes[k]))
-            if key not in cache:
-                S = np.asarray(_mesh.sinh_space(key[0], spot_max, spotdensity, key[1],
-                                                force_exact=force_exact), dtype=np.float64)
-                cache[key] = (S, int(np.argmin(np.abs(S - key[0]))))
-            S, i = cache[key]
-            spots[self.p_off[k]:self.p_off[k + 1]] = S
-            idx[k] = self.p_off[k] + i
+        # one mesh per distinct (spot, size), placed at every option that has it
+        keys = np.stack([spot, self.sizes.astype(np.float64)], axis=1)
+        uniq, inv = np.unique(keys, axis=0, return_inverse=True)
+        inv = inv.reshape(-1)
+        for u, (s0, m) in enumerate(uniq):
+            S = np.asarray(_mesh.sinh_space(float(s0), spot_max, spotdensity, int(m),
+                                            force_exact=force_exact), dtype=np.float64)
+            which = np.nonzero(inv == u)[0]
+            spots[self.p_off[which][:, None] + np.arange(int(m))] = S
+            idx[which] = self.p_off[which] + int(np.argmin(np.abs(S - s0)))
         if not hasattr(self, "_h"):
             pin = lambda t: t.pin_memory()
             self._h = dict(spots=pin(torch.empty(self.total_points, dtype=torch.float64)),

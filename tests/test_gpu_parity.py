@@ -347,7 +347,10 @@ def test_blackscholes_engine(cuda, golden):
     r, var, K = g["params"]
     opt = Option(spot=100., strike=K, interest_rate=r, variance=var, tenor=1.0)
     grid = Grid([g["S"]], initializer=lambda x: np.maximum(x - K, 0))
-    F = BlackScholesFiniteDifferenceEngine(opt, grid=grid)
+    # the per-operator path: every solve starts from the engine's initial grid
+    # (the fused path keeps its last result as the next start, like the
+    # reference GPU engine's in-place device grid)
+    F = BlackScholesFiniteDifferenceEngine(opt, grid=grid, fused=False)
     n, dt = 200, 1.0 / 200
     for name, fn in (("implicit", lambda: F.solve_implicit(n, dt)),
                      ("douglas", lambda: F.solve_douglas(n, dt, theta=0.5)),
