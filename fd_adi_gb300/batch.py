@@ -688,18 +688,18 @@ class BlackScholesBatch(object):
         spot = np.broadcast_to(np.asarray(spot, dtype=np.float64), (n,))
         params = np.ascontiguousarray(params, dtype=np.float64).reshape(n, 2)
         dt = np.broadcast_to(np.asarray(dt, dtype=np.float64), (n,))
-        spots = np.empty(self.total_points)
-        idx = np.empty(n, dtype=np.int64)
-        # one mesh per distinct (spot, size), placed at every option that has it
-        keys = np.stack([spot, self.sizes.astype(np.float64)], axis=1)
-        uniq, inv = np.unique(keys, axis=0, return_inverse=True)
+        # one mesh per distinct (spot, size), laid out option after option
+        su, si = np.unique(spot, return_inverse=True)
+        mx = int(self.sizes.max()) + 1
+        ku, inv = np.unique(si.reshape(-1).astype(np.int64) * mx + self.sizes,
+                            return_inverse=True)
         inv = inv.reshape(-1)
-        for u, (s0, m) in enumerate(uniq):
-            S = np.asarray(_mesh.sinh_space(float(s0), spot_max, spotdensity, int(m),
-                                            force_exact=force_exact), dtype=np.float64)
-            which = np.nonzero(inv == u)[0]
-            spots[self.p_off[which][:, None] + np.arange(int(m))] = S
-            idx[which] = self.p_off[which] + int(np.argmin(np.abs(S - s0)))
+        uniq = [(float(su[k // mx]), int(k % mx)) for k in ku]
+        ms = [np.asarray(_mesh.sinh_space(s0, spot_max, spotdensity, m,
+                                          force_exact=force_exact), dtype=np.float64)
+              for s0, m in uniq]
+        at = np.array([int(np.argmin(np.abs(S - s0))) for S, (s0, _) in zip(ms, uniq)])
+        idx = self.p_off[:-1] + at[inv]
         if not hasattr(self, "_h"):
             pin = lambda t: t.pin_memory()
             self._h = dict(spots=pin(torch.empty(self.total_points, dtype=torch.float64)),
@@ -714,7 +714,7 @@ class BlackScholesBatch(object):
                            V=torch.empty(self.total_points, dtype=torch.float64,
                                          device=self.device))
         h, d = self._h, self._d
-        h["spots"].numpy()[:] = spots
+        np.concatenate([ms[u] for u in inv], out=h["spots"].numpy())
         h["params"].numpy()[:] = params.reshape(-1)
         h["dt"].numpy()[:] = dt
         h["K"].numpy()[:] = strikes
