@@ -442,7 +442,7 @@ def run_surrogate(args):
     import torch
     from fd_adi_gb300 import _lib
     from fd_adi_gb300.surrogate import (Surrogate, adi_price, sobol_queries, BOX_LO, BOX_HI,
-                                        MLPEnsemble, LAYERS)
+                                        MLPEnsemble, LAYERS, CoarseADI)
     torch.cuda.set_device(0)
     _lib.load()
     dev = torch.device("cuda", 0)
@@ -480,12 +480,25 @@ def run_surrogate(args):
         alt["cv%d_heldout_rms_abs_err" % cv] = float(np.sqrt(np.mean((pa - pte) ** 2)))
         alt["cv%d_heldout_max_abs_err" % cv] = float(np.abs(pa - pte).max())
         del s_alt
-    sur = Surrogate(members=4, seed=args.seed, device=dev, cv=args.cv)
+    coarse = ctr = cte = None
+    t_coarse = None
+    if args.coarse:
+        # two-level surrogate: the coarse-grid ADI prices of the training and
+        # held-out draws (their control variate), priced and timed here
+        nS_c, nv_c, nt_c = (int(x) for x in args.coarse.split("x"))
+        coarse = CoarseADI(nS_c, nv_c, nt_c)
+        t0 = time.perf_counter()
+        ctr = coarse.price(Qtr)
+        cte = coarse.price(Qte)
+        torch.cuda.synchronize()
+        t_coarse = time.perf_counter() - t0
+        print("coarse prices: %.1f s" % t_coarse, file=sys.stderr, flush=True)
+    sur = Surrogate(members=4, seed=args.seed, device=dev, cv=args.cv, coarse=coarse)
     t0 = time.perf_counter()
-    sur.fit(Qtr, ptr, dtr, epochs=args.epochs, batch=8192, lr=1e-3)
+    sur.fit(Qtr, ptr, dtr, epochs=args.epochs, batch=8192, lr=1e-3, coarse=ctr)
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
-    p, d, spread, fb, _ = sur.predict(torch.as_tensor(Qte, device=dev))
+    p, d, spread, fb, _ = sur.predict(torch.as_tensor(Qte, device=dev), coarse=cte)
     p = p.cpu().numpy()
     d = d.cpu().numpy()
     err = np.abs(p - pte)
@@ -495,10 +508,12 @@ def run_surrogate(args):
         # calibrated on the first half of the held-out draws; judged on the
         # second half and on the served query sample below
         t0 = time.perf_counter()
-        sur.fit_gate(Qtr, ptr, epochs=args.epochs, batch=8192, lr=1e-3)
+        sur.fit_gate(Qtr, ptr, epochs=args.epochs, batch=8192, lr=1e-3, coarse=ctr)
         h = Qte.shape[0] // 2
-        tau, cal_fb = sur.calibrate(Qte[:h], pte[:h], bar=1e-3, margin=args.gate_margin)
-        _, _, _, fbv, _ = sur.predict(torch.as_tensor(Qte[h:], device=dev))
+        tau, cal_fb = sur.calibrate(Qte[:h], pte[:h], bar=1e-3, margin=args.gate_margin,
+                                    coarse=None if cte is None else cte[:h])
+        _, _, _, fbv, _ = sur.predict(torch.as_tensor(Qte[h:], device=dev),
+                                      coarse=None if cte is None else cte[h:])
         fbv = fbv.cpu().numpy().astype(bool)
         ev = err[h:]
         gate = {"bar": 1e-3, "threshold_log10": tau, "margin_log10": args.gate_margin,
@@ -520,8 +535,10 @@ def run_surrogate(args):
         return sur.price(Q, pool=pool, **grid)
 
     def serve():
+        # warm-up on the first 16,384 queries: graphs and plans are built
+        # there, and a full warm-up pass would price every fallback twice
         for _ in range(args.warmup):
-            step()
+            sur.price(Q[:min(nq, 16384)], pool=pool, **grid)
         torch.cuda.synchronize()
         times = []
         for _ in range(args.steps):
@@ -531,7 +548,10 @@ def run_surrogate(args):
             times.append(time.perf_counter() - t0)
         return nq / float(np.mean(times)), times, pq, dq, fbq
 
+    if gate is not None:
+        print("gate: %s" % json.dumps(gate), file=sys.stderr, flush=True)
     value, times, pq, dq, fbq = serve()
+    print("served: %.1f options/s" % value, file=sys.stderr, flush=True)
     # accuracy of the served prices on a sample, against FP64 ADI
     ns = min(args.sample, nq)
     sidx = np.linspace(0, nq - 1, ns).astype(int)
@@ -551,7 +571,7 @@ def run_surrogate(args):
     # tensor pipe: one ensemble forward on the query batch, timed with events
     Qd = torch.as_tensor(Q, device=dev)
     M = (nq // 128) * 128
-    X, _, _ = sur.feat(Qd[:M].contiguous())
+    X, _, _ = sur.feat(Qd[:M].contiguous())   # the network's cost is the same either way
     sur.net.infer(X, M)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
@@ -590,13 +610,20 @@ def run_surrogate(args):
                           "query_rms_abs_err": float(np.sqrt(np.mean(qerr ** 2))),
                           "batched_adi_options_per_s": adi_rate,
                           "speedup_vs_batched_adi": value / adi_rate,
-                          "control_variate": ("Black-Scholes at mean variance" if args.cv == 0
+                          "control_variate": (("FP64 ADI on a %s grid (price), Black-Scholes "
+                                               "at mean variance (delta)" % args.coarse)
+                                              if args.coarse else
+                                              "Black-Scholes at mean variance" if args.cv == 0
                                               else "Black-Scholes at mean variance + order-%d "
                                               "series in vol of variance (price), residual / "
                                               "(sigma sqrt T + 0.1)" % args.cv),
                           **alt,
                           "error_gate": gate,
                           "box_gate_only": box_only,
+                          "coarse_adi": (None if coarse is None else
+                                         {"grid": args.coarse, "price_s_train_and_test": t_coarse,
+                                          "options_per_s": (Qtr.shape[0] + Qte.shape[0])
+                                          / t_coarse}),
                           "adam_betas": list(sur.net.adam[:2]),
                           "train_data": cached or "priced in this run",
                           "data_gen_s": t_data, "train_s": t_train,
@@ -947,6 +974,9 @@ def main():
                     help="surrogate: train and calibrate the error gate (served error <= 1e-3)")
     ap.add_argument("--gate-margin", type=float, default=0.05,
                     help="error gate: threshold margin below the calibration misses (log10)")
+    ap.add_argument("--coarse", default=None,
+                    help="surrogate: two-level variant, the coarse-ADI control variate's grid "
+                         "as NSxNVxNT (e.g. 128x64x80)")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))

@@ -142,6 +142,50 @@ def test_surrogate_learns_adi_prices_and_gates(dev):
     assert t_sur * 100 < t_adi
 
 
+def test_two_level_surrogate_beats_the_single_level(dev):
+    """The coarse-ADI control variate: CoarseADI prices are the batched ADI's
+    on the coarse grid; trained on the same 4096 draws, the two-level
+    surrogate's held-out error is well below the single-level one's (the
+    network only learns the fine - coarse difference, 0.01 RMS here);
+    out-of-box queries fall back; the host box test equals the device's."""
+    from fd_adi_gb300.surrogate import Surrogate, CoarseADI, adi_price, sobol_queries, in_box
+    fine = dict(nS=64, nv=32, nt=40)
+    Qtr = sobol_queries(4096, seed=1)
+    Qte = sobol_queries(512, seed=2)
+    ptr, dtr = adi_price(Qtr, **fine)
+    pte, _ = adi_price(Qte, **fine)
+    co = CoarseADI(48, 24, 40, chunk=1024)
+    ctr, cte = co.price(Qtr), co.price(Qte)
+    ref, _ = adi_price(Qte[:100], nS=48, nv=24, nt=40)
+    np.testing.assert_allclose(cte[:100], ref, rtol=1e-12, atol=1e-12)
+    errs = {}
+    for name, coarse in (("one", None), ("two", co)):
+        sur = Surrogate(members=4, seed=0, device=dev, coarse=coarse)
+        sur.net.adam = (0.9, 0.999, 1e-8)
+        sur.fit(Qtr, ptr, dtr, epochs=40, batch=512, lr=2e-3,
+                coarse=ctr if coarse is not None else None)
+        p = sur.predict(torch.as_tensor(Qte, device=dev),
+                        coarse=cte if coarse is not None else None)[0].cpu().numpy()
+        errs[name] = float(np.sqrt(np.mean((p - pte) ** 2)))
+        if coarse is not None:
+            two = sur
+    assert errs["two"] < 0.5 * errs["one"], errs
+    with pytest.raises(ValueError):
+        two.predict(torch.as_tensor(Qte, device=dev))
+    # price(): the coarse prices are computed inside; out-of-box queries
+    # (T beyond the box) fall back to the fine ADI and get its price
+    Qm = Qte[:64].copy()
+    Qm[:16, 2] = 4.0
+    ib = in_box(Qm)
+    assert not ib[:16].any() and ib[16:].all()
+    _, _, dev_inbox = two.features(torch.as_tensor(Qm, device=dev), np.ones(64))
+    np.testing.assert_array_equal(dev_inbox.cpu().numpy().astype(bool), ib)
+    p, _, fbh = two.price(Qm, **fine)
+    assert fbh[:16].all()
+    pf, _ = adi_price(Qm[:16], **fine)
+    np.testing.assert_allclose(p[:16], pf, rtol=1e-12)
+
+
 @pytest.mark.parametrize("tiles", [200, 33, 1])
 def test_fused_inference_matches_layered_forward(dev, tiles):
     """The one-kernel inference against the layer-by-layer tensor-core forward
