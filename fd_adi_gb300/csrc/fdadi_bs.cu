@@ -307,7 +307,7 @@ __device__ __forceinline__ void back_into(const BsLine &l, double dp, int k, int
 // Douglas (and Craig-Sneyd, which in one dimension without a mixed term
 // repeats the Douglas sweep and keeps its result): V <- Li^-1 (V + F V - Le V).
 // Row 0 is the Dirichlet row, forced to 0 (d'_0 = 0).
-template <int PF>
+template <int PF, int PFB>
 __device__ void bs_douglas(const BsLine &l, double rf) {
     const int n = l.n;
     double xm = 0.0, x0 = l.at(1, BA_V), dp = 0.0;
@@ -323,7 +323,7 @@ __device__ void bs_douglas(const BsLine &l, double rf) {
             xm = x0;
             x0 = r.xp;
         });
-    back_into<PF>(l, dp, BA_V, BA_LM);
+    back_into<PFB>(l, dp, BA_V, BA_LM);
 }
 
 struct ImplicitRow {
@@ -332,7 +332,7 @@ struct ImplicitRow {
 
 // Implicit step: V <- (1 - dt' A)^-1 (V - R_i) with the residual on the
 // S_max row (solve, BandedOperator.pyx:364-394).
-template <int PF>
+template <int PF, int PFB>
 __device__ void bs_implicit(const BsLine &l, double ri) {
     const int n = l.n;
     double dp = 0.0;
@@ -345,7 +345,7 @@ __device__ void bs_implicit(const BsLine &l, double ri) {
             dp = (y - r.a * dp) * r.inv;
             l.at(i, BA_D) = dp;
         });
-    back_into<PF>(l, dp, BA_V, BA_LI);
+    back_into<PFB>(l, dp, BA_V, BA_LI);
 }
 
 // HV in one dimension (FiniteDifferenceEngine.pyx:700-775):
@@ -355,7 +355,7 @@ __device__ void bs_implicit(const BsLine &l, double ri) {
 // no mixed term:
 //   Y0 = V + F V, Y1 = Li^-1 (Y0 - Le V),
 //   V <- Li^-1 (Y0 + (1/2 - theta) F (Y1 - V) - Le V), F with its residual.
-template <bool MCS, int PF>
+template <bool MCS, int PF, int PFB>
 __device__ void bs_two_sweeps(const BsLine &l, double rf, double c) {
     const int n = l.n;
     const double v1 = l.at(1, BA_V);
@@ -374,7 +374,7 @@ __device__ void bs_two_sweeps(const BsLine &l, double rf, double c) {
             xm = x0;
             x0 = r.xp;
         });
-    back_into<PF>(l, dp, BA_Y1, BA_LM);
+    back_into<PFB>(l, dp, BA_Y1, BA_LM);
     // second sweep: differences D = V - Y1 (HV) or Y1 - V (MCS), each formed
     // once and carried along the window; the Dirichlet row's is forced to 0
     const double y1 = l.at(1, BA_Y1);
@@ -402,7 +402,7 @@ __device__ void bs_two_sweeps(const BsLine &l, double rf, double c) {
             ym = y0r; y0r = yp;
             dm = d0; d0 = dpn;
         });
-    back_into<PF>(l, dp, BA_V, BA_LM);
+    back_into<PFB>(l, dp, BA_V, BA_LM);
 }
 
 struct BsSched {
@@ -412,10 +412,14 @@ struct BsSched {
 
 // One thread per slot: copy the option's packed state into its interleaved
 // line, run the whole schedule, copy the result back.
-// Four blocks per SM (at most 128 registers a thread): 65,536 options (2048
-// warps) stay resident in one wave.
-template <int PF>
-__global__ void __launch_bounds__(BS_THREADS, 4) bs_run_kernel(BsArena A, double *Vp, BsSched sc) {
+// PF rows ahead in the forward sweeps, PFB in the back substitutions (one
+// FP64 instruction a row: it needs more rows in flight to cover the same
+// latency). MINB blocks per SM: four (at most 128 registers a thread) keep
+// 65,536 options (2048 warps) resident in one wave; one, for batches with
+// fewer warps than SMs, leaves the registers to a deep prefetch.
+template <int PF, int PFB, int MINB>
+__global__ void __launch_bounds__(BS_THREADS, MINB) bs_run_kernel(BsArena A, double *Vp,
+                                                                  BsSched sc) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= A.S) return;
     if (A.slot_opt[s] < 0) return;
@@ -423,12 +427,12 @@ __global__ void __launch_bounds__(BS_THREADS, 4) bs_run_kernel(BsArena A, double
     double *src = Vp + A.slot_soff[s];
     for (int i = 0; i < l.n; ++i) l.at(i, BA_V) = src[i];
     const double rf = A.RF[s], ri = A.RI[s];
-    for (int k = 0; k < sc.implicit_steps; ++k) bs_implicit<PF>(l, ri);
+    for (int k = 0; k < sc.implicit_steps; ++k) bs_implicit<PF, PFB>(l, ri);
     const double c = 0.5 - sc.theta;
     for (int k = 0; k < sc.n_steps; ++k) {
-        if (sc.scheme == FDADI_SCHEME_HV) bs_two_sweeps<false, PF>(l, rf, c);
-        else if (sc.scheme == FDADI_SCHEME_MCS) bs_two_sweeps<true, PF>(l, rf, c);
-        else bs_douglas<PF>(l, rf);
+        if (sc.scheme == FDADI_SCHEME_HV) bs_two_sweeps<false, PF, PFB>(l, rf, c);
+        else if (sc.scheme == FDADI_SCHEME_MCS) bs_two_sweeps<true, PF, PFB>(l, rf, c);
+        else bs_douglas<PF, PFB>(l, rf);
     }
     for (int i = 0; i < l.n; ++i) src[i] = l.at(i, BA_V);
 }
@@ -507,17 +511,22 @@ int fdadi_bs_run(const fdadi_bs_batch_t *b, void *ws, int64_t bytes, double *V, 
     int rc = bs_begin(b, ws, bytes, L);
     if (rc) return rc;
     FDADI_REQUIRE(V != nullptr, "null state");
-    FDADI_REQUIRE(b->prefetch >= 0 && b->prefetch <= 2,
-                  "prefetch must be 0 (by batch size), 1 or 2");
+    FDADI_REQUIRE(b->prefetch == 0 || b->prefetch == 1 || b->prefetch == 2 || b->prefetch == 16,
+                  "prefetch must be 0 (by batch size), 1, 2 or 16");
     BsSched sc{b->scheme, b->n_steps, b->implicit_steps, b->theta};
-    // rows in flight per thread: two rows ahead measured faster at both 4096
-    // options (212 against 239 ms for 200 HV steps) and 65,536 (325 against 364)
-    const int pf = b->prefetch == 0 ? 2 : b->prefetch;
+    // rows in flight per thread: two ahead measured faster than one at both
+    // 4096 options (212 against 239 ms for 200 HV steps) and 65,536 (325
+    // against 364); with fewer warps than SMs each warp is alone on its SM and
+    // the deep variant (2 ahead in the sweeps, 16 in the back substitutions,
+    // one block per SM for the registers) hides more of the memory latency
+    int pf = b->prefetch;
+    if (pf == 0) pf = L.n_groups < sm_count() ? 16 : 2;
     const unsigned grid = (L.S + BS_THREADS - 1) / BS_THREADS;
     cudaStream_t st = as_stream(stream);
     const BsArena A = bs_view(L, (char *)ws);
-    if (pf == 1) bs_run_kernel<1><<<grid, BS_THREADS, 0, st>>>(A, V, sc);
-    else bs_run_kernel<2><<<grid, BS_THREADS, 0, st>>>(A, V, sc);
+    if (pf == 1) bs_run_kernel<1, 1, 4><<<grid, BS_THREADS, 0, st>>>(A, V, sc);
+    else if (pf == 2) bs_run_kernel<2, 2, 4><<<grid, BS_THREADS, 0, st>>>(A, V, sc);
+    else bs_run_kernel<2, 16, 1><<<grid, BS_THREADS, 0, st>>>(A, V, sc);
     FDADI_CHECK_LAUNCH();
     return FDADI_OK;
 }
