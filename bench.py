@@ -827,7 +827,7 @@ def run_bs(args):
 
     run_ms = run_once()
     by_pf = {}
-    for pf in (1, 2, 16):
+    for pf in (2, 4, 8):
         batch.struct.prefetch = pf
         by_pf[str(pf)] = round(run_once(), 3)
     batch.struct.prefetch = 0

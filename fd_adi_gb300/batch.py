@@ -529,9 +529,8 @@ class BlackScholesBatch(object):
     then ``n_steps`` of ``scheme`` ("douglas", "hv", "cs" or "mcs") at ``theta``.
     The operator is the reference's (blackscholes.py:144-239): r S D_S +
     1/2 var S^2 D_SS - r, U = 0 at the first mesh point, dU/dS = 1 at S_max.
-    prefetch: rows each thread loads ahead in its sweeps (1, 2, or 16 for the
-    deep variant of small batches; 0 chooses by batch size); the results do
-    not depend on it."""
+    prefetch: rows each thread keeps in flight in its sweeps (2, 4 or 8; 0
+    chooses by batch size); the results do not depend on it."""
 
     def __init__(self, options, meshes, scheme="hv", n_steps=1, dt=0.01, theta=HV_THETA,
                  implicit_steps=0, implicit_dt_factor=0.5, device=None, stream=None,

@@ -21,6 +21,10 @@
 // stored operator rows keep the per-step work free of the multiplications
 // that building F and Le would cost, and the rows' own rounding (a
 // coefficient rounded differently would bias every step the same way).
+//
+// A thread's rows stream from HBM (a large batch's rows do not fit in L2)
+// and each row's arithmetic is short, so the sweeps keep several rows in
+// flight: cp.async copies into a per-thread ring in shared memory.
 #include <algorithm>
 #include <vector>
 
@@ -226,29 +230,46 @@ struct BsLine {
     __device__ __forceinline__ double &at(int i, int k) const { return p[(int64_t)i * RS + k * ST]; }
 };
 
-// Rows are loaded PF ahead of the row being eliminated: every row's loads are
-// independent of the recurrence, so PF of them stay in flight while the
-// thread computes (one thread walks a whole line; with few options per SM
-// nothing else would hide the memory latency). Runs body(i, row) for
-// i = lo, lo + dir, ... (count rows), row = load(i).
-template <int PF, class Row, class Load, class Body>
-__device__ __forceinline__ void pipelined(int lo, int count, int dir, Load load, Body body) {
-    Row ring[PF];
-#pragma unroll
-    for (int d = 0; d < PF; ++d)
-        if (d < count) ring[d] = load(lo + d * dir);
-    for (int k0 = 0; k0 < count; k0 += PF) {
-#pragma unroll
-        for (int d = 0; d < PF; ++d) {
-            const int k = k0 + d;
-            if (k < count) {
-                body(lo + k * dir, ring[d]);
-                if (k + PF < count) ring[d] = load(lo + (k + PF) * dir);
-            }
-        }
-    }
+// ---- asynchronous row ring -------------------------------------------------
+//
+// Every row's operands are independent of the recurrence, so they can be
+// fetched long before the row is eliminated. Each thread keeps a ring of
+// rows in shared memory, filled by cp.async (8-byte copies, no registers
+// held while they fly): value v of ring slot s of lane l at
+// ring[(s * RING_W + v) * 32 + l]. PF rows are in flight in the forward
+// sweeps, PFB in the back substitutions (two values a row, one FP64
+// instruction: the same latency needs more rows). A thread reads only what
+// its own copies wrote, after waiting for them, so no barrier is needed.
+constexpr int RING_W = 11;  // values a forward-sweep row needs (second HV sweep)
+
+__device__ __forceinline__ void cp_async8(double *dst, const double *src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
+// Runs body(i, slot) for i = lo, lo + dir, ... (count rows), slot holding
+// row i as issue(i, slot) requested it (NV values, stride 32). PF: power of 2.
+template <int PF, int NV, class Issue, class Body>
+__device__ __forceinline__ void ring_sweep(double *ring, int lo, int count, int dir, Issue issue,
+                                           Body body) {
+#pragma unroll
+    for (int d = 0; d < PF; ++d) {
+        if (d < count) issue(lo + d * dir, ring + d * NV * 32);
+        cp_commit();
+    }
+    for (int k = 0; k < count; ++k) {
+        cp_wait<PF - 1>();
+        double *slot = ring + (k & (PF - 1)) * NV * 32;
+        body(lo + k * dir, slot);
+        if (k + PF < count) issue(lo + (k + PF) * dir, slot);
+        cp_commit();
+    }
+}
 
 // y = c x on row i (1 <= i <= n-1) with x[-1] forced to the Dirichlet value 0
 // (apply, BandedOperator.pyx:331-361: force_dirichlet, then the DIA
@@ -259,47 +280,45 @@ __device__ __forceinline__ double row_apply(double sub, double mid, double sup, 
     return fma(sub, xm, acc);
 }
 
-// One row's operands in a forward sweep: the next state value(s), the rows
-// of F and Le, the elimination factors and (second HV sweep) Y0.
-struct SweepRow {
-    double xp, yp, y0, f0, f1, f2, e0, e1, e2, a, inv;
-};
-
+// Forward-sweep row operands: slot values 0..8 = V[i+1], F (3), Le (3),
+// elimination factors (sub, 1/m); the second HV sweep adds Y1[i+1] and Y0[i]
+// at 9 and 10. On the last row the "next" values are fetched from the row
+// itself (always inside the line) and ignored.
 template <bool WITH_Y>
-__device__ __forceinline__ SweepRow load_sweep(const BsLine &l, int i) {
+__device__ __forceinline__ void issue_sweep(const BsLine &l, int i, double *slot) {
     const double *q = l.p + (int64_t)i * RS;
-    const bool top = i == l.n - 1;
-    SweepRow r;
-    r.xp = top ? 0.0 : q[RS + BA_V * ST];
-    r.yp = (WITH_Y && !top) ? q[RS + BA_Y1 * ST] : 0.0;
-    r.y0 = WITH_Y ? q[BA_Y0 * ST] : 0.0;
-    r.f0 = q[BA_F * ST];
-    r.f1 = q[(BA_F + 1) * ST];
-    r.f2 = top ? 0.0 : q[(BA_F + 2) * ST];
-    r.e0 = q[BA_LE * ST];
-    r.e1 = q[(BA_LE + 1) * ST];
-    r.e2 = top ? 0.0 : q[(BA_LE + 2) * ST];
-    r.a = q[BA_LM * ST];
-    r.inv = q[(BA_LM + 1) * ST];
-    return r;
+    const double *nx = i == l.n - 1 ? q : q + RS;
+    cp_async8(slot, nx + BA_V * ST);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        cp_async8(slot + (1 + k) * 32, q + (BA_F + k) * ST);
+        cp_async8(slot + (4 + k) * 32, q + (BA_LE + k) * ST);
+    }
+    cp_async8(slot + 7 * 32, q + BA_LM * ST);
+    cp_async8(slot + 8 * 32, q + (BA_LM + 1) * ST);
+    if (WITH_Y) {
+        cp_async8(slot + 9 * 32, nx + BA_Y1 * ST);
+        cp_async8(slot + 10 * 32, q + BA_Y0 * ST);
+    }
 }
-
-struct BackRow {
-    double d, cp;
-};
 
 // Back substitution x_i = d'_i - c'_i x_{i+1} into array k (factors of
 // array fac), from x_{n-1} = d'_{n-1} = dp.
-template <int PF>
-__device__ __forceinline__ void back_into(const BsLine &l, double dp, int k, int fac) {
+template <int PFB>
+__device__ __forceinline__ void back_into(const BsLine &l, double *ring, double dp, int k,
+                                          int fac) {
     const int n = l.n;
     l.at(n - 1, k) = dp;
     double x = dp;
-    pipelined<PF, BackRow>(
-        n - 2, n - 1, -1,
-        [&](int i) { return BackRow{l.at(i, BA_D), l.at(i, fac + 2)}; },
-        [&](int i, const BackRow &r) {
-            x = r.d - r.cp * x;
+    ring_sweep<PFB, 2>(
+        ring, n - 2, n - 1, -1,
+        [&](int i, double *slot) {
+            const double *q = l.p + (int64_t)i * RS;
+            cp_async8(slot, q + BA_D * ST);
+            cp_async8(slot + 32, q + (fac + 2) * ST);
+        },
+        [&](int i, const double *slot) {
+            x = slot[0] - slot[32] * x;
             l.at(i, k) = x;
         });
 }
@@ -308,44 +327,46 @@ __device__ __forceinline__ void back_into(const BsLine &l, double dp, int k, int
 // repeats the Douglas sweep and keeps its result): V <- Li^-1 (V + F V - Le V).
 // Row 0 is the Dirichlet row, forced to 0 (d'_0 = 0).
 template <int PF, int PFB>
-__device__ void bs_douglas(const BsLine &l, double rf) {
+__device__ void bs_douglas(const BsLine &l, double *ring, double rf) {
     const int n = l.n;
     double xm = 0.0, x0 = l.at(1, BA_V), dp = 0.0;
     l.at(0, BA_D) = 0.0;
-    pipelined<PF, SweepRow>(
-        1, n - 1, 1, [&](int i) { return load_sweep<false>(l, i); },
-        [&](int i, const SweepRow &r) {
+    ring_sweep<PF, RING_W>(
+        ring, 1, n - 1, 1, [&](int i, double *slot) { issue_sweep<false>(l, i, slot); },
+        [&](int i, const double *r) {
             const bool top = i == n - 1;
-            double y = x0 + (row_apply(r.f0, r.f1, r.f2, top, xm, x0, r.xp) + (top ? rf : 0.0));
-            y = y - row_apply(r.e0, r.e1, r.e2, top, xm, x0, r.xp);
-            dp = (y - r.a * dp) * r.inv;
+            const double xp = top ? 0.0 : r[0];
+            double y = x0 + (row_apply(r[32], r[64], r[96], top, xm, x0, xp) + (top ? rf : 0.0));
+            y = y - row_apply(r[128], r[160], r[192], top, xm, x0, xp);
+            dp = (y - r[224] * dp) * r[256];
             l.at(i, BA_D) = dp;
             xm = x0;
-            x0 = r.xp;
+            x0 = xp;
         });
-    back_into<PFB>(l, dp, BA_V, BA_LM);
+    back_into<PFB>(l, ring, dp, BA_V, BA_LM);
 }
-
-struct ImplicitRow {
-    double v, a, inv;
-};
 
 // Implicit step: V <- (1 - dt' A)^-1 (V - R_i) with the residual on the
 // S_max row (solve, BandedOperator.pyx:364-394).
 template <int PF, int PFB>
-__device__ void bs_implicit(const BsLine &l, double ri) {
+__device__ void bs_implicit(const BsLine &l, double *ring, double ri) {
     const int n = l.n;
     double dp = 0.0;
     l.at(0, BA_D) = 0.0;
-    pipelined<PF, ImplicitRow>(
-        1, n - 1, 1,
-        [&](int i) { return ImplicitRow{l.at(i, BA_V), l.at(i, BA_LI), l.at(i, BA_LI + 1)}; },
-        [&](int i, const ImplicitRow &r) {
-            const double y = i == n - 1 ? r.v - ri : r.v;
-            dp = (y - r.a * dp) * r.inv;
+    ring_sweep<PF, 3>(
+        ring, 1, n - 1, 1,
+        [&](int i, double *slot) {
+            const double *q = l.p + (int64_t)i * RS;
+            cp_async8(slot, q + BA_V * ST);
+            cp_async8(slot + 32, q + BA_LI * ST);
+            cp_async8(slot + 64, q + (BA_LI + 1) * ST);
+        },
+        [&](int i, const double *r) {
+            const double y = i == n - 1 ? r[0] - ri : r[0];
+            dp = (y - r[32] * dp) * r[64];
             l.at(i, BA_D) = dp;
         });
-    back_into<PFB>(l, dp, BA_V, BA_LI);
+    back_into<PFB>(l, ring, dp, BA_V, BA_LI);
 }
 
 // HV in one dimension (FiniteDifferenceEngine.pyx:700-775):
@@ -356,53 +377,54 @@ __device__ void bs_implicit(const BsLine &l, double ri) {
 //   Y0 = V + F V, Y1 = Li^-1 (Y0 - Le V),
 //   V <- Li^-1 (Y0 + (1/2 - theta) F (Y1 - V) - Le V), F with its residual.
 template <bool MCS, int PF, int PFB>
-__device__ void bs_two_sweeps(const BsLine &l, double rf, double c) {
+__device__ void bs_two_sweeps(const BsLine &l, double *ring, double rf, double c) {
     const int n = l.n;
     const double v1 = l.at(1, BA_V);
     double xm = 0.0, x0 = v1, dp = 0.0;
     l.at(0, BA_D) = 0.0;
-    pipelined<PF, SweepRow>(
-        1, n - 1, 1, [&](int i) { return load_sweep<false>(l, i); },
-        [&](int i, const SweepRow &r) {
+    ring_sweep<PF, RING_W>(
+        ring, 1, n - 1, 1, [&](int i, double *slot) { issue_sweep<false>(l, i, slot); },
+        [&](int i, const double *r) {
             const bool top = i == n - 1;
+            const double xp = top ? 0.0 : r[0];
             const double y0 =
-                x0 + (row_apply(r.f0, r.f1, r.f2, top, xm, x0, r.xp) + (top ? rf : 0.0));
+                x0 + (row_apply(r[32], r[64], r[96], top, xm, x0, xp) + (top ? rf : 0.0));
             l.at(i, BA_Y0) = y0;
-            const double z = y0 - row_apply(r.e0, r.e1, r.e2, top, xm, x0, r.xp);
-            dp = (z - r.a * dp) * r.inv;
+            const double z = y0 - row_apply(r[128], r[160], r[192], top, xm, x0, xp);
+            dp = (z - r[224] * dp) * r[256];
             l.at(i, BA_D) = dp;
             xm = x0;
-            x0 = r.xp;
+            x0 = xp;
         });
-    back_into<PFB>(l, dp, BA_Y1, BA_LM);
+    back_into<PFB>(l, ring, dp, BA_Y1, BA_LM);
     // second sweep: differences D = V - Y1 (HV) or Y1 - V (MCS), each formed
     // once and carried along the window; the Dirichlet row's is forced to 0
     const double y1 = l.at(1, BA_Y1);
     double vm = 0.0, v0 = v1, ym = 0.0, y0r = y1;
     double dm = 0.0, d0 = MCS ? y0r - v0 : v0 - y0r;
     dp = 0.0;
-    pipelined<PF, SweepRow>(
-        1, n - 1, 1, [&](int i) { return load_sweep<true>(l, i); },
-        [&](int i, const SweepRow &r) {
+    ring_sweep<PF, RING_W>(
+        ring, 1, n - 1, 1, [&](int i, double *slot) { issue_sweep<true>(l, i, slot); },
+        [&](int i, const double *r) {
             const bool top = i == n - 1;
-            const double vp = r.xp, yp = r.yp;
+            const double vp = top ? 0.0 : r[0], yp = top ? 0.0 : r[288];
             const double dpn = top ? 0.0 : (MCS ? yp - vp : vp - yp);
-            const double fd = row_apply(r.f0, r.f1, r.f2, top, dm, d0, dpn);
+            const double fd = row_apply(r[32], r[64], r[96], top, dm, d0, dpn);
             double w;
             if (MCS) {
-                w = fma(c, fd + (top ? rf : 0.0), r.y0);
-                w = w - row_apply(r.e0, r.e1, r.e2, top, vm, v0, vp);
+                w = fma(c, fd + (top ? rf : 0.0), r[320]);
+                w = w - row_apply(r[128], r[160], r[192], top, vm, v0, vp);
             } else {
-                w = fma(-0.5, fd, r.y0);
-                w = w - row_apply(r.e0, r.e1, r.e2, top, ym, y0r, yp);
+                w = fma(-0.5, fd, r[320]);
+                w = w - row_apply(r[128], r[160], r[192], top, ym, y0r, yp);
             }
-            dp = (w - r.a * dp) * r.inv;
+            dp = (w - r[224] * dp) * r[256];
             l.at(i, BA_D) = dp;
             vm = v0; v0 = vp;
             ym = y0r; y0r = yp;
             dm = d0; d0 = dpn;
         });
-    back_into<PFB>(l, dp, BA_V, BA_LM);
+    back_into<PFB>(l, ring, dp, BA_V, BA_LM);
 }
 
 struct BsSched {
@@ -412,14 +434,17 @@ struct BsSched {
 
 // One thread per slot: copy the option's packed state into its interleaved
 // line, run the whole schedule, copy the result back.
-// PF rows ahead in the forward sweeps, PFB in the back substitutions (one
-// FP64 instruction a row: it needs more rows in flight to cover the same
-// latency). MINB blocks per SM: four (at most 128 registers a thread) keep
-// 65,536 options (2048 warps) resident in one wave; one, for batches with
-// fewer warps than SMs, leaves the registers to a deep prefetch.
+// PF rows in flight in the forward sweeps, PFB in the back substitutions,
+// held in a shared-memory ring of PF * RING_W values per thread. MINB blocks
+// per SM: four keep 65,536 options (2048 warps) resident in one wave; one,
+// for batches with fewer warps than SMs, leaves shared memory to a deeper
+// ring.
 template <int PF, int PFB, int MINB>
 __global__ void __launch_bounds__(BS_THREADS, MINB) bs_run_kernel(BsArena A, double *Vp,
                                                                   BsSched sc) {
+    static_assert(PFB * 2 <= PF * RING_W, "back ring must fit the forward ring");
+    extern __shared__ double bs_ring[];
+    double *ring = bs_ring + (threadIdx.x / 32) * (PF * RING_W * 32) + (threadIdx.x & 31);
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= A.S) return;
     if (A.slot_opt[s] < 0) return;
@@ -427,14 +452,25 @@ __global__ void __launch_bounds__(BS_THREADS, MINB) bs_run_kernel(BsArena A, dou
     double *src = Vp + A.slot_soff[s];
     for (int i = 0; i < l.n; ++i) l.at(i, BA_V) = src[i];
     const double rf = A.RF[s], ri = A.RI[s];
-    for (int k = 0; k < sc.implicit_steps; ++k) bs_implicit<PF, PFB>(l, ri);
+    for (int k = 0; k < sc.implicit_steps; ++k) bs_implicit<PF, PFB>(l, ring, ri);
     const double c = 0.5 - sc.theta;
     for (int k = 0; k < sc.n_steps; ++k) {
-        if (sc.scheme == FDADI_SCHEME_HV) bs_two_sweeps<false, PF, PFB>(l, rf, c);
-        else if (sc.scheme == FDADI_SCHEME_MCS) bs_two_sweeps<true, PF, PFB>(l, rf, c);
-        else bs_douglas<PF, PFB>(l, rf);
+        if (sc.scheme == FDADI_SCHEME_HV) bs_two_sweeps<false, PF, PFB>(l, ring, rf, c);
+        else if (sc.scheme == FDADI_SCHEME_MCS) bs_two_sweeps<true, PF, PFB>(l, ring, rf, c);
+        else bs_douglas<PF, PFB>(l, ring, rf);
     }
     for (int i = 0; i < l.n; ++i) src[i] = l.at(i, BA_V);
+}
+
+template <int PF, int PFB, int MINB>
+int launch_run(const BsArena &A, double *V, const BsSched &sc, unsigned grid, cudaStream_t st) {
+    const size_t smem = (size_t)BS_THREADS * PF * RING_W * sizeof(double);
+    if (smem > 48 * 1024)
+        FDADI_CUDA(cudaFuncSetAttribute(bs_run_kernel<PF, PFB, MINB>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    bs_run_kernel<PF, PFB, MINB><<<grid, BS_THREADS, smem, st>>>(A, V, sc);
+    FDADI_CHECK_LAUNCH();
+    return FDADI_OK;
 }
 
 // One block per option: V = max(S - K, 0) or max(K - S, 0).
@@ -511,24 +547,20 @@ int fdadi_bs_run(const fdadi_bs_batch_t *b, void *ws, int64_t bytes, double *V, 
     int rc = bs_begin(b, ws, bytes, L);
     if (rc) return rc;
     FDADI_REQUIRE(V != nullptr, "null state");
-    FDADI_REQUIRE(b->prefetch == 0 || b->prefetch == 1 || b->prefetch == 2 || b->prefetch == 16,
-                  "prefetch must be 0 (by batch size), 1, 2 or 16");
+    FDADI_REQUIRE(b->prefetch == 0 || b->prefetch == 2 || b->prefetch == 4 || b->prefetch == 8,
+                  "prefetch must be 0 (by batch size), 2, 4 or 8");
     BsSched sc{b->scheme, b->n_steps, b->implicit_steps, b->theta};
-    // rows in flight per thread: two ahead measured faster than one at both
-    // 4096 options (212 against 239 ms for 200 HV steps) and 65,536 (325
-    // against 364); with fewer warps than SMs each warp is alone on its SM and
-    // the deep variant (2 ahead in the sweeps, 16 in the back substitutions,
-    // one block per SM for the registers) hides more of the memory latency
+    // rows in flight: 4 (16 in the back substitutions; 44 KB of ring a block,
+    // four blocks an SM) where the warps fill the SMs; with fewer warps than
+    // SMs each warp is alone on its SM, and 8 (32) hide more of the latency
     int pf = b->prefetch;
-    if (pf == 0) pf = L.n_groups < sm_count() ? 16 : 2;
+    if (pf == 0) pf = L.n_groups < sm_count() ? 8 : 4;
     const unsigned grid = (L.S + BS_THREADS - 1) / BS_THREADS;
     cudaStream_t st = as_stream(stream);
     const BsArena A = bs_view(L, (char *)ws);
-    if (pf == 1) bs_run_kernel<1, 1, 4><<<grid, BS_THREADS, 0, st>>>(A, V, sc);
-    else if (pf == 2) bs_run_kernel<2, 2, 4><<<grid, BS_THREADS, 0, st>>>(A, V, sc);
-    else bs_run_kernel<2, 16, 1><<<grid, BS_THREADS, 0, st>>>(A, V, sc);
-    FDADI_CHECK_LAUNCH();
-    return FDADI_OK;
+    if (pf == 2) return launch_run<2, 8, 4>(A, V, sc, grid, st);
+    if (pf == 4) return launch_run<4, 16, 4>(A, V, sc, grid, st);
+    return launch_run<8, 32, 1>(A, V, sc, grid, st);
 }
 
 int fdadi_bs_payoff(const fdadi_bs_batch_t *b, void *ws, int64_t bytes, const double *strikes,

@@ -347,10 +347,10 @@ typedef struct fdadi_bs_batch {
     const double *spots;     /* DEVICE [sum n] spot meshes, packed */
     const double *params;    /* DEVICE [n_options][2]: r, variance sigma^2 */
     const double *dt;        /* DEVICE [n_options] main-segment step */
-    int32_t prefetch;        /* rows each thread loads ahead in its line sweeps: 1 or 2;
-                              * 16: 2 in the forward sweeps and 16 in the back
-                              * substitutions (for batches of fewer warps than SMs);
-                              * 0: chosen by batch size. Results are identical. */
+    int32_t prefetch;        /* rows each thread keeps in flight in its forward sweeps
+                              * (2, 4 or 8; four times as many in the back
+                              * substitutions), copied asynchronously into shared
+                              * memory; 0: chosen by batch size. Results are identical. */
     int32_t reserved;
 } fdadi_bs_batch_t;
 

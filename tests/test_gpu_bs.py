@@ -116,7 +116,7 @@ def test_uneven_batch_vs_oracle(cuda, scheme):
     V0 = [np.maximum(S - o["K"], 0.0) for o, S in zip(opts, meshes)]
     got = b.solve(V0)
     # both prefetch depths run the same arithmetic: identical bits
-    for pf in (1, 2, 16):
+    for pf in (2, 4, 8):
         other = BlackScholesBatch([(o["r"], o["var"]) for o in opts], meshes, dt=dts,
                                   prefetch=pf, **kw).solve(V0)
         for x, y in zip(got, other):

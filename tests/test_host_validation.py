@@ -192,6 +192,6 @@ def test_black_scholes_batch_is_validated():
     # the argument checks of the other entry points come before any launch
     assert lib.fdadi_bs_prepare(ctypes.byref(b), None, got, None) != 0
     assert lib.fdadi_bs_run(ctypes.byref(b), FAKE, got - 1, FAKE, None) == 3
-    b.prefetch = 4
+    b.prefetch = 3
     assert lib.fdadi_bs_run(ctypes.byref(b), FAKE, got, FAKE, None) == 1
     assert "prefetch" in _lib.last_error()
