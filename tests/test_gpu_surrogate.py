@@ -117,10 +117,10 @@ def test_surrogate_learns_adi_prices_and_gates(dev):
     # half of the held-out draws so that every query there whose price misses
     # the bar (the median error here: this short training is coarse) falls
     # back; on the other half its scores must rank misses above hits
-    sur.fit_gate(Qtr, ptr, epochs=40, batch=512, lr=2e-3)
     h = Qte.shape[0] // 2
     e = np.abs(p - pte)
     bar = float(np.median(e[:h]))
+    sur.fit_gate(Qtr, ptr, epochs=40, batch=512, lr=2e-3, floor=0.2 * bar)
     tau, frac = sur.calibrate(Qte[:h], pte[:h], bar=bar, margin=0.0)
     _, _, _, fbg, cntg = sur.predict(torch.as_tensor(Qte, device=dev))
     fbg = fbg.cpu().numpy().astype(bool)
