@@ -435,10 +435,9 @@ struct BsSched {
 // One thread per slot: copy the option's packed state into its interleaved
 // line, run the whole schedule, copy the result back.
 // PF rows in flight in the forward sweeps, PFB in the back substitutions,
-// held in a shared-memory ring of PF * RING_W values per thread. MINB blocks
-// per SM: four keep 65,536 options (2048 warps) resident in one wave; one,
-// for batches with fewer warps than SMs, leaves shared memory to a deeper
-// ring.
+// held in a shared-memory ring of PF * RING_W values per thread. MINB: the
+// blocks per SM the registers must allow (the ring's shared memory allows
+// four blocks at PF 4, two at PF 8).
 template <int PF, int PFB, int MINB>
 __global__ void __launch_bounds__(BS_THREADS, MINB) bs_run_kernel(BsArena A, double *Vp,
                                                                   BsSched sc) {
@@ -550,17 +549,17 @@ int fdadi_bs_run(const fdadi_bs_batch_t *b, void *ws, int64_t bytes, double *V, 
     FDADI_REQUIRE(b->prefetch == 0 || b->prefetch == 2 || b->prefetch == 4 || b->prefetch == 8,
                   "prefetch must be 0 (by batch size), 2, 4 or 8");
     BsSched sc{b->scheme, b->n_steps, b->implicit_steps, b->theta};
-    // rows in flight: 4 (16 in the back substitutions; 44 KB of ring a block,
-    // four blocks an SM) where the warps fill the SMs; with fewer warps than
-    // SMs each warp is alone on its SM, and 8 (32) hide more of the latency
-    int pf = b->prefetch;
-    if (pf == 0) pf = L.n_groups < sm_count() ? 8 : 4;
+    // rows in flight: 8 (32 in the back substitutions; 88 KB of ring a block)
+    // measured fastest at 65,536 options (199 ms against 266 ms with 4 and
+    // 265 ms with 2, although it allows two blocks an SM instead of four) and
+    // level with the others at 4096 and 16,384
+    const int pf = b->prefetch == 0 ? 8 : b->prefetch;
     const unsigned grid = (L.S + BS_THREADS - 1) / BS_THREADS;
     cudaStream_t st = as_stream(stream);
     const BsArena A = bs_view(L, (char *)ws);
     if (pf == 2) return launch_run<2, 8, 4>(A, V, sc, grid, st);
     if (pf == 4) return launch_run<4, 16, 4>(A, V, sc, grid, st);
-    return launch_run<8, 32, 1>(A, V, sc, grid, st);
+    return launch_run<8, 32, 2>(A, V, sc, grid, st);
 }
 
 int fdadi_bs_payoff(const fdadi_bs_batch_t *b, void *ws, int64_t bytes, const double *strikes,
