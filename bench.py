@@ -505,7 +505,7 @@ def run_surrogate(args):
     gate = None
     if args.gate:
         # the error gate, trained on the training draws' own errors and
-        # calibrated on the first half of the held-out draws; judged on the
+        # calibrated on the first half of the held-out draws; evaluated on the
         # second half and on the served query sample below
         t0 = time.perf_counter()
         sur.fit_gate(Qtr, ptr, epochs=args.epochs, batch=8192, lr=1e-3, coarse=ctr)

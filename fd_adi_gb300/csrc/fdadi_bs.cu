@@ -227,7 +227,9 @@ __global__ void bs_build_kernel(BsArena A, BsBuild a) {
 struct BsLine {
     double *p;
     int n;
-    __device__ __forceinline__ double &at(int i, int k) const { return p[(int64_t)i * RS + k * ST]; }
+    __device__ __forceinline__ double &at(int i, int k) const {
+        return p[(int64_t)i * RS + k * ST];
+    }
 };
 
 // ---- asynchronous row ring -------------------------------------------------
@@ -236,7 +238,8 @@ struct BsLine {
 // fetched long before the row is eliminated. Each thread keeps a ring of
 // rows in shared memory, filled by cp.async (8-byte copies, no registers
 // held while they fly): value v of ring slot s of lane l at
-// ring[(s * RING_W + v) * 32 + l]. PF rows are in flight in the forward
+// ring[(s * NV + v) * 32 + l], NV the values a row of that sweep needs
+// (the ring holds RING_W of them a slot). PF rows are in flight in the forward
 // sweeps, PFB in the back substitutions (two values a row, one FP64
 // instruction: the same latency needs more rows). A thread reads only what
 // its own copies wrote, after waiting for them, so no barrier is needed.
@@ -246,7 +249,9 @@ __device__ __forceinline__ void cp_async8(double *dst, const double *src) {
     const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
 }
-__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_commit() {
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
 template <int N>
 __device__ __forceinline__ void cp_wait() {
     asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");

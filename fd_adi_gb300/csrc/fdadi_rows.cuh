@@ -109,8 +109,8 @@ static __device__ Row3 spot_row_w(const double *w, int64_t SS, const double *S, 
 struct Thomas {
     double cp = 0.0;
     bool bad = false;
-    __device__ __forceinline__ void row(double *L, int64_t stride, int64_t q, double sub, double mid,
-                                        double sup, bool first) {
+    __device__ __forceinline__ void row(double *L, int64_t stride, int64_t q, double sub,
+                                        double mid, double sup, bool first) {
         const double m = first ? mid : SUB(mid, MUL(sub, cp));
         const double inv = DIV(1.0, m);
         if (!isfinite(inv)) bad = true;
