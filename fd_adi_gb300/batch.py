@@ -508,6 +508,30 @@ def payoff_grids(options, meshes):
             for o, m in zip(options, meshes)]
 
 
+def bs_meshes_batch(spot, sizes, spot_max=1500.0, spotdensity=7.0, force_exact=True, out=None):
+    """The Black-Scholes engine's meshes for a batch (blackscholes.py:181-183:
+    sinh_space(spot, spot_max, spotdensity, n, force_exact)), one per distinct
+    (spot, size) and laid out option after option into out (a new array if
+    None), bit-identical to building each option's; and each option's price
+    index into that layout, the mesh point nearest its spot
+    (blackscholes.py:222-228). Returns the indices."""
+    sizes = np.asarray(sizes, dtype=np.int64).reshape(-1)
+    spot = np.broadcast_to(np.asarray(spot, dtype=np.float64), sizes.shape)
+    p_off = np.concatenate([[0], np.cumsum(sizes)])
+    if out is None:
+        out = np.empty(int(p_off[-1]))
+    su, si = np.unique(spot, return_inverse=True)
+    mx = int(sizes.max()) + 1
+    ku, inv = np.unique(si.reshape(-1).astype(np.int64) * mx + sizes, return_inverse=True)
+    inv = inv.reshape(-1)
+    uniq = [(float(su[k // mx]), int(k % mx)) for k in ku]
+    ms = [np.asarray(_mesh.sinh_space(s0, spot_max, spotdensity, m, force_exact=force_exact),
+                     dtype=np.float64) for s0, m in uniq]
+    at = np.array([int(np.argmin(np.abs(S - s0))) for S, (s0, _) in zip(ms, uniq)])
+    np.concatenate([ms[u] for u in inv], out=out)
+    return p_off[:-1] + at[inv]
+
+
 def bs_params(opt):
     """(r, variance) of a Black-Scholes Option or a 2-sequence."""
     if hasattr(opt, "interest_rate"):
@@ -688,18 +712,6 @@ class BlackScholesBatch(object):
         spot = np.broadcast_to(np.asarray(spot, dtype=np.float64), (n,))
         params = np.ascontiguousarray(params, dtype=np.float64).reshape(n, 2)
         dt = np.broadcast_to(np.asarray(dt, dtype=np.float64), (n,))
-        # one mesh per distinct (spot, size), laid out option after option
-        su, si = np.unique(spot, return_inverse=True)
-        mx = int(self.sizes.max()) + 1
-        ku, inv = np.unique(si.reshape(-1).astype(np.int64) * mx + self.sizes,
-                            return_inverse=True)
-        inv = inv.reshape(-1)
-        uniq = [(float(su[k // mx]), int(k % mx)) for k in ku]
-        ms = [np.asarray(_mesh.sinh_space(s0, spot_max, spotdensity, m,
-                                          force_exact=force_exact), dtype=np.float64)
-              for s0, m in uniq]
-        at = np.array([int(np.argmin(np.abs(S - s0))) for S, (s0, _) in zip(ms, uniq)])
-        idx = self.p_off[:-1] + at[inv]
         if not hasattr(self, "_h"):
             pin = lambda t: t.pin_memory()
             self._h = dict(spots=pin(torch.empty(self.total_points, dtype=torch.float64)),
@@ -714,7 +726,8 @@ class BlackScholesBatch(object):
                            V=torch.empty(self.total_points, dtype=torch.float64,
                                          device=self.device))
         h, d = self._h, self._d
-        np.concatenate([ms[u] for u in inv], out=h["spots"].numpy())
+        idx = bs_meshes_batch(spot, self.sizes, spot_max, spotdensity, force_exact,
+                              out=h["spots"].numpy())
         h["params"].numpy()[:] = params.reshape(-1)
         h["dt"].numpy()[:] = dt
         h["K"].numpy()[:] = strikes
