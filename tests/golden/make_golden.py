@@ -260,6 +260,11 @@ def blackscholes():
     out["douglas"] = H.quiet(F.solve_douglas, 200, 1.0 / 200, initial=V0, theta=0.5)
     out["hv"] = H.quiet(F.solve_hundsdorferverwer, 200, 1.0 / 200, initial=V0, theta=0.5)
     out["smooth"] = H.quiet(F.solve_smooth, 200, 1.0 / 200, initial=V0, smoothing_steps=1)
+    # Craig-Sneyd in one dimension: cross_term is 0 without a mixed operator
+    # (FiniteDifferenceEngine.pyx:595-613), so the original scheme repeats the
+    # Douglas sweep; the modified one adds (1/2 - theta) F(Y2 - V)
+    out["cs"] = H.quiet(F.solve_craigsneyd, 200, 1.0 / 200, initial=V0, theta=0.5)
+    out["mcs"] = H.quiet(F.solve_craigsneyd2, 200, 1.0 / 200, initial=V0, theta=1.0 / 3)
     np.savez_compressed(os.path.join(HERE, "blackscholes.npz"), **out)
 
 

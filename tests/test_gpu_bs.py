@@ -39,6 +39,8 @@ GOLDEN_SCHED = {
     "hv": lambda n, dt: dict(scheme="hv", n_steps=n, theta=0.5),
     "smooth": lambda n, dt: dict(scheme="hv", n_steps=n - 1, theta=0.6, implicit_steps=2,
                                  implicit_dt_factor=0.5),
+    "cs": lambda n, dt: dict(scheme="cs", n_steps=n, theta=0.5),
+    "mcs": lambda n, dt: dict(scheme="mcs", n_steps=n, theta=1.0 / 3),
 }
 
 
@@ -64,7 +66,8 @@ def test_engine_vs_reference_fixture(cuda, golden, fused):
 
 def test_batch_of_copies_matches_fixture(cuda, golden):
     """70 copies of the reference case in one batch (three warp groups, the
-    last one ragged): every copy equals the fixture under every schedule."""
+    last one ragged): every copy equals the fixture under every schedule,
+    Craig-Sneyd and modified Craig-Sneyd included."""
     from fd_adi_gb300.batch import BlackScholesBatch
     g = golden("blackscholes")
     r, var, K = g["params"]

@@ -84,9 +84,13 @@ def test_blackscholes(golden):
     for name, sched in (("implicit", [("implicit", n, dt, 1.0)]),
                         ("douglas", [("douglas", n, dt, 0.5)]),
                         ("hv", [("hv", n, dt, 0.5)]),
-                        ("smooth", [("implicit", 2, dt / 2, 1.0), ("hv", n - 1, dt, 0.6)])):
+                        ("smooth", [("implicit", 2, dt / 2, 1.0), ("hv", n - 1, dt, 0.6)]),
+                        ("cs", [("cs", n, dt, 0.5)]),
+                        ("mcs", [("mcs", n, dt, 1.0 / 3)])):
         out = O.bs_solve(g["S"], r, var, g["V0"], sched)
         assert np.abs(out - g[name]).max() <= 1e-11 * np.abs(g[name]).max(), name
+    # one-dimensional Craig-Sneyd repeats the Douglas sweep in the reference
+    np.testing.assert_array_equal(g["cs"], g["douglas"])
     i = int(np.argmin(np.abs(g["S"] - 100.0)))
     exact = analytic.bs_call(100.0, K, r, var, 1.0)[0]
     assert abs(g["douglas"][i] - exact) <= 1e-3 * exact
