@@ -498,14 +498,15 @@ class HestonBatch(object):
             out = torch.empty(flat_idx.numel(), dtype=torch.float64, device=self.device)
         _lib.call("fdadi_gather", ctypes.c_void_p(V.data_ptr()),
                   ctypes.c_void_p(flat_idx.data_ptr()), ctypes.c_void_p(out.data_ptr()),
-                  flat_idx.numel(), ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream))
+                  flat_idx.numel(),
+                  ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream))
         return out
 
 
 def payoff_grids(options, meshes):
     """Call payoff max(S - K, 0) on each option's grid (heston.py:402)."""
-    return [np.maximum(np.asarray(m[0])[:, None] - o.strike, 0.0) * np.ones((1, np.asarray(m[1]).size))
-            for o, m in zip(options, meshes)]
+    return [np.maximum(np.asarray(m[0])[:, None] - o.strike, 0.0)
+            * np.ones((1, np.asarray(m[1]).size)) for o, m in zip(options, meshes)]
 
 
 def bs_meshes_batch(spot, sizes, spot_max=1500.0, spotdensity=7.0, force_exact=True, out=None):

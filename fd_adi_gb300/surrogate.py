@@ -85,7 +85,8 @@ class MLPEnsemble(object):
             W = torch.zeros(self.P, N, K)
             gain = math.sqrt(2.0) if li < len(LAYERS) - 1 else 0.5
             a = gain * math.sqrt(3.0 / k_valid)
-            W[:, :n_valid, :k_valid] = (torch.rand(self.P, n_valid, k_valid, generator=g) * 2 - 1) * a
+            u = torch.rand(self.P, n_valid, k_valid, generator=g)
+            W[:, :n_valid, :k_valid] = (u * 2 - 1) * a
             self.W.append(W.to(self.dev))
             self.b.append(torch.zeros(self.P, N, device=self.dev))
             self.Wb.append(self.W[-1].to(torch.bfloat16))
@@ -112,7 +113,8 @@ class MLPEnsemble(object):
         if M not in self._bufs:
             P, d = self.P, self.dev
             b = {"Y": [torch.empty(P, M, N, dtype=torch.float32, device=d) for _, N in LAYERS],
-                 "H": [torch.empty(P, M, N, dtype=torch.bfloat16, device=d) for _, N in LAYERS[:-1]],
+                 "H": [torch.empty(P, M, N, dtype=torch.bfloat16, device=d)
+                       for _, N in LAYERS[:-1]],
                  "dY": [torch.empty(P, M, N, dtype=torch.bfloat16, device=d) for _, N in LAYERS],
                  "dYT": torch.empty(P, 256, M, dtype=torch.bfloat16, device=d),
                  "XT": torch.empty(P, 256, M, dtype=torch.bfloat16, device=d),
@@ -269,7 +271,8 @@ def adi_price(queries, nS=256, nv=128, nt=200, chunk=4096, graph=False, spot_max
     delta = np.empty(n)
     jobs = [(q[k, 0], q[k, 1], q[k, 8], nS, nv, spot_max_factor * q[k, 1], var_max)
             for k in range(n)]
-    meshes = pool.map(_mesh_job, jobs, chunksize=64) if pool is not None else [_mesh_job(j) for j in jobs]
+    meshes = (pool.map(_mesh_job, jobs, chunksize=64) if pool is not None
+              else [_mesh_job(j) for j in jobs])
     for c0 in range(0, n, chunk):
         sl = slice(c0, min(n, c0 + chunk))
         qs = q[sl]

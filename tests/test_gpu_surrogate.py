@@ -80,7 +80,8 @@ def test_training_gradients_match_cpu_oracle(dev):
                 scale = ref.abs().max().item()
                 assert (got - ref).abs().max().item() <= tol * scale, (mimic, p, l)
                 gotb = bufs["db"][l][p].cpu().to(torch.float64)
-                assert (gotb - gb[p][l]).abs().max().item() <= tol * gb[p][l].abs().max().item() + 1e-12
+                bound = tol * gb[p][l].abs().max().item() + 1e-12
+                assert (gotb - gb[p][l]).abs().max().item() <= bound
 
 
 def test_surrogate_learns_adi_prices_and_gates(dev):
