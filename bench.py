@@ -632,6 +632,25 @@ def run_surrogate(args):
     return 0
 
 
+def _ref_worker_init(barrier):
+    """Pool initializer of the reference-engine workers: import the compiled
+    reference, then wait until every worker has."""
+    from oracle import ref_harness as H
+    H._import()
+    barrier.wait(timeout=600)
+
+
+def _warm_job(job):
+    """A short copy of a reference-engine job (a few time steps, no grid kept)
+    for warming a worker."""
+    j = list(job)
+    j[8] = j[8] * 4 / j[11]   # T scaled with the steps, as cpu_baseline does
+    j[11] = 4
+    if len(j) > 12:
+        j[12] = False
+    return tuple(j)
+
+
 def cpu_baseline(w, n_sample, nt_sample=None, want_results=False):
     """The reference CPU engine (compiled from its generated sources on this
     host, kind "reference") or, where it does not import, the C restatement
@@ -655,8 +674,13 @@ def cpu_baseline(w, n_sample, nt_sample=None, want_results=False):
         jobs = [(w["S0"], w["K"][k], w["r"][k], w["kappa"][k], w["theta"][k], w["sigma"][k],
                  w["rho"][k], w["v0"][k], w["T"][k] * nrun / nt, w["nS"][k], w["nv"][k], nrun,
                  want_results) for k in idx]
-        with mp.get_context("spawn").Pool(min(cores, len(jobs))) as pool:
-            pool.map(H.price_option, jobs[:1])       # warm the workers' imports
+        workers = min(cores, len(jobs))
+        ctx = mp.get_context("spawn")
+        # every worker imports the reference engine and waits for the others
+        # before it takes a job, so no import falls in the timed region
+        with ctx.Pool(workers, initializer=_ref_worker_init,
+                      initargs=(ctx.Barrier(workers),)) as pool:
+            pool.map(H.price_option, [_warm_job(jobs[0])] * workers, chunksize=1)
             t0 = time.perf_counter()
             res = pool.map(H.price_option, jobs, chunksize=1)
             dt = time.perf_counter() - t0
@@ -714,9 +738,39 @@ def parity(batch, V, prices, sample):
             "ok": bool(max(prel) <= 1e-10 and (not grel or max(grel) <= 1e-9))}
 
 
+def run_reference_bs(args):
+    """The reference arm of the Black-Scholes workload: the reference CPU
+    engine on a bounded sample of the same options, per step."""
+    w = workload_bs(args.bs_options, args.seed)
+    rates, elapsed = [], []
+    for s in range(args.warmup + args.steps):
+        cb, _, _ = bs_cpu_baseline(w, args.ref_sample)
+        if s >= args.warmup:
+            rates.append(cb["value"])
+            elapsed.append(cb["elapsed_s"])
+    value = float(np.mean(rates))
+    cb["value"] = value
+    line = {"metric": "Black-Scholes options/sec, batched FP64 ADI", "value": value,
+            "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": float(np.mean(elapsed)) * 1e3,
+            "ms_per_workload_extrapolated": len(w["K"]) / value * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": "batched Black-Scholes calls, uneven meshes, HV nt=200 "
+                                   "with Rannacher start", "options": len(w["K"]),
+                       "nt": w["nt"], "nS": "uniform {64..512 step 32}", "seed": args.seed},
+            "cpu_baseline": cb,
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return 0
+    if args.workload == "bs":
+        return run_reference_bs(args)
     w = workload_large() if args.workload == "large" else workload(args.options, args.seed)
     rates, elapsed = [], []
     for s in range(args.warmup + args.steps):
@@ -877,48 +931,69 @@ def run_bs(args):
                                 "peak_source": peak_src}},
            "fp64_probe": probe, "clocks": clk}
     if args.cpu_sample > 0:
-        from oracle import ref_harness as H
-        idx = sorted(set(np.linspace(0, n - 1, args.cpu_sample).astype(int).tolist()))
-        cores = os.cpu_count() or 1
-        if H.available():
-            for var in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
-                os.environ[var] = "1"
-            jobs = [(100.0, w["K"][k], w["r"][k], w["var"][k], w["T"][k], int(w["nS"][k]), nt)
-                    for k in idx]
-            with mp.get_context("spawn").Pool(min(cores, len(jobs))) as pool:
-                pool.map(H.price_bs_option, jobs[:1])
-                t0 = time.perf_counter()
-                res = pool.map(H.price_bs_option, jobs, chunksize=4)
-                el = time.perf_counter() - t0
-            ref = np.array([x[0] for x in res])
-            kind = "reference"
-            what = "reference CPU engine (compat build) with blackscholes.py's operator"
-        else:
-            from oracle import oracle as O
-            t0 = time.perf_counter()
-            ref = np.array([O.bs_solve(meshes[k], w["r"][k], w["var"][k],
-                                       np.maximum(meshes[k] - w["K"][k], 0.0),
-                                       [("implicit", 2, dts[k] / 2, 1.0),
-                                        ("hv", nt - 1, dts[k], HV_THETA)])[
-                                int(flat_idx[k].item() - batch.p_off[k])] for k in idx])
-            el = time.perf_counter() - t0
-            cores = 1
-            kind = "port"
-            what = "C restatement of the reference engine (oracle), one core"
-        mean_pts = float(np.mean(w["nS"]))
-        pts = float(sum(int(w["nS"][k]) for k in idx)) * nt
+        cb, idx, ref = bs_cpu_baseline(w, args.cpu_sample)
         got = prices.cpu().numpy()[idx]
         rel = np.abs(got - ref) / np.abs(ref)
-        out["cpu_baseline"] = {"value": pts / el / (mean_pts * nt), "unit": UNIT,
-                               "cores": min(cores, len(idx)), "kind": kind, "elapsed_s": el,
-                               "sample": "%s: %d options spread through the %d-option "
-                                         "workload on %d cores in %.1f s, scaled to the "
-                                         "workload's mean option"
-                                         % (what, len(idx), n, min(cores, len(idx)), el)}
+        out["cpu_baseline"] = cb
         out["parity"] = {"n": len(idx), "max_price_rel": float(rel.max()), "price_bar": 1e-10,
                          "ok": bool(rel.max() <= 1e-10)}
     print(json.dumps(out))
     return 0
+
+
+def bs_cpu_baseline(w, n_sample):
+    """The reference CPU engine with blackscholes.py's operator (compat build,
+    kind "reference") or, where it does not import, the C oracle (kind
+    "port"), on n_sample options spread through the Black-Scholes workload,
+    one single-threaded process per host core. Returns the baseline object,
+    the sample's option indices and its prices."""
+    import multiprocessing as mp
+    from oracle import ref_harness as H
+    from fd_adi_gb300 import mesh as M
+    n = len(w["K"])
+    nt = w["nt"]
+    idx = sorted(set(np.linspace(0, n - 1, n_sample).astype(int).tolist()))
+    cores = os.cpu_count() or 1
+    if H.available():
+        for var in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
+            os.environ[var] = "1"
+        jobs = [(100.0, w["K"][k], w["r"][k], w["var"][k], w["T"][k], int(w["nS"][k]), nt)
+                for k in idx]
+        workers = min(cores, len(jobs))
+        ctx = mp.get_context("spawn")
+        with ctx.Pool(workers, initializer=_ref_worker_init,
+                      initargs=(ctx.Barrier(workers),)) as pool:
+            pool.map(H.price_bs_option, [jobs[0]] * workers, chunksize=1)
+            t0 = time.perf_counter()
+            res = pool.map(H.price_bs_option, jobs, chunksize=4)
+            el = time.perf_counter() - t0
+        ref = np.array([x[0] for x in res])
+        kind = "reference"
+        what = "reference CPU engine (compat build) with blackscholes.py's operator"
+    else:
+        from oracle import oracle as O
+        ref = []
+        t0 = time.perf_counter()
+        for k in idx:
+            S = np.asarray(M.sinh_space(100.0, 1500.0, 7.0, int(w["nS"][k]), force_exact=True))
+            dt = w["T"][k] / nt
+            g = O.bs_solve(S, w["r"][k], w["var"][k], np.maximum(S - w["K"][k], 0.0),
+                           [("implicit", 2, dt / 2, 1.0), ("hv", nt - 1, dt, HV_THETA)])
+            ref.append(g[int(np.argmin(np.abs(S - 100.0)))])
+        el = time.perf_counter() - t0
+        ref = np.array(ref)
+        cores = 1
+        kind = "port"
+        what = "C restatement of the reference engine (oracle), one core"
+    used = min(cores, len(idx))
+    mean_pts = float(np.mean(w["nS"]))
+    pts = float(sum(int(w["nS"][k]) for k in idx)) * nt
+    cb = {"value": pts / el / (mean_pts * nt), "unit": UNIT, "cores": used, "kind": kind,
+          "elapsed_s": el,
+          "sample": "%s: %d options spread through the %d-option workload on %d cores in "
+                    "%.1f s, scaled to the workload's mean option"
+                    % (what, len(idx), n, used, el)}
+    return cb, idx, ref
 
 
 def config_block(args, w):
