@@ -6,7 +6,9 @@ reference's ``HestonFiniteDifferenceEngine`` does. ``heston.py`` itself cannot
 be imported under Python 3 (print statements, numexpr, pylab), so its
 coefficient dict (heston.py:302-333), boundary dict (heston.py:335-359) and
 grid construction (heston.py:380-406) are restated here in Python 3 and handed
-to the reference ``FiniteDifferenceEngineADI`` unchanged.
+to the reference ``FiniteDifferenceEngineADI`` unchanged. The Black-Scholes
+engine's coefficient and boundary dicts (blackscholes.py:197-219) are
+restated the same way (``price_bs_option``).
 
 Usable where the reference was compat-built from its sources
 (``oracle/build_ref.py``) or where its generated C/C++ was compiled
